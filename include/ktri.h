@@ -1,0 +1,159 @@
+/*
+ * ktri.h — C ABI of the katric_gb300 exact local triangle-counting engine (sm_103a).
+ *
+ * The engine replaces the local counting phase of KaTric (degree-based orientation,
+ * per-vertex id sort, edge-iterator set intersection) with CUDA kernels on one GPU.
+ * Input: an undirected simple graph in CSR form, u64 first_out[n+1] and u32 head[nnz],
+ * both directions of every edge stored, no self-loops, no duplicate entries, adjacency
+ * lists in any order.  Output: the u64 triangle total and, optionally, u64 per-vertex
+ * counts (each triangle {v,u,w} adds one to v, u and w).
+ *
+ * Every function returns an int status: KTRI_OK (0) or a negative KTRI_ERR_* code.
+ * No C++ exception crosses this boundary.  Reference paths below are relative to the
+ * KaTric source tree.
+ */
+#ifndef KTRI_H
+#define KTRI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KTRI_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define KTRI_OK 0
+#define KTRI_ERR_INVALID_ARGUMENT (-1) /* null pointer, size mismatch, bad option */
+#define KTRI_ERR_INVALID_CSR (-2)      /* id >= n, self-loop, non-monotone first_out, duplicate */
+#define KTRI_ERR_OUT_OF_MEMORY (-3)    /* device or host allocation failed, or over the memory budget */
+#define KTRI_ERR_CUDA (-4)             /* a CUDA runtime call failed; see ktri_last_error */
+#define KTRI_ERR_TIMEOUT (-5)          /* a bounded device-side wait gave up */
+#define KTRI_ERR_UNSUPPORTED (-6)      /* valid input outside what this build handles */
+#define KTRI_ERR_IO (-7)               /* file could not be read or written, or is malformed */
+#define KTRI_ERR_NO_DEVICE (-8)        /* no CUDA device, or the requested one does not exist */
+
+/* ---- options ------------------------------------------------------------------------- */
+/* Intersection strategy, mirroring Config::intersection_method (include/cetric/config.h:172,
+ * selected by shmetric's --intersection-method, apps/parse_parameters.h:156-158).
+ * KTRI_METHOD_AUTO is the GPU default: owner-side shared-memory hash tables that stream the
+ * shorter out-list of every edge.  The other four run the reference's strategies on
+ * id-sorted out-lists, one warp per oriented edge.  All five give identical counts. */
+#define KTRI_METHOD_AUTO 0
+#define KTRI_METHOD_MERGE 1         /* merge_intersection, include/cetric/counters/intersection.h:82-96 */
+#define KTRI_METHOD_BINARY_SEARCH 2 /* binary_search_intersection, intersection.h:99-117 */
+#define KTRI_METHOD_BINARY 3        /* binary_intersection, intersection.h:120-192 */
+#define KTRI_METHOD_HYBRID 4        /* hybrid rule, intersection.h:66-77 */
+
+typedef struct ktri_opts {
+    uint32_t struct_size;          /* sizeof(ktri_opts); 0 is read as "all defaults" */
+    int32_t intersection_method;   /* KTRI_METHOD_* */
+    uint32_t small_outdegree;      /* owners with out-degree <= this use the tile kernel (0 = tuned default) */
+    uint32_t collect_stats;        /* 1: also compute wedge_checks / intersection work counters */
+    uint64_t binary_intersection_cutoff; /* Config::binary_intersection_cutoff (config.h:173), default 1000 */
+    double hybrid_cutoff_scale;    /* Config::hybrid_cutoff_scale (config.h:174), default 1.0 */
+    uint32_t reserved[8];
+} ktri_opts;
+
+/* Counters of the last run on a context, named after the reference's Statistics fields
+ * (include/cetric/statistics.h:193-199) where one exists. */
+typedef struct ktri_run_stats {
+    uint64_t triangles;               /* stats.local.local_triangles */
+    uint64_t n;                       /* vertices */
+    uint64_t nnz;                     /* stored adjacency entries (2m) */
+    uint64_t oriented_edges;          /* m: out-list entries after orientation */
+    uint64_t wedge_checks;            /* sum over oriented (v,u) of |N+(u)| (collect_stats) */
+    uint64_t intersection_size_local; /* sum over oriented (v,u) of |N+(v)|+|N+(u)| (collect_stats) */
+    uint64_t streamed_entries;        /* out-list entries the AUTO kernels stream (collect_stats) */
+    uint32_t input_sorted;            /* 1 when every input adjacency list was strictly increasing */
+    uint32_t method;                  /* strategy that ran */
+    float ms_orient;                  /* device time of orientation (+ sort when one ran) */
+    float ms_count;                   /* device time of intersection + reduction */
+    float ms_total;                   /* device time of the whole call */
+    float ms_count_small;             /* AUTO: device time of the small-owner tile kernel */
+    float ms_count_large;             /* AUTO: device time of the large-owner vertex kernel */
+    uint32_t reserved[3];
+} ktri_run_stats;
+
+typedef struct ktri_ctx ktri_ctx;
+
+/* ---- context ---------------------------------------------------------------------------- */
+/* A context binds one CUDA device, owns a grow-only device workspace (oriented CSR, tables,
+ * counters) and a pinned host staging buffer.  Calls on one context are serialised by the
+ * caller; different contexts may be used from different threads. */
+int ktri_ctx_create(int device, ktri_ctx** out);
+int ktri_ctx_destroy(ktri_ctx* ctx);
+/* Cap on the workspace this context may hold (bytes; 0 = no cap).  Over-budget calls fail
+ * with KTRI_ERR_OUT_OF_MEMORY before launching anything. */
+int ktri_ctx_set_memory_budget(ktri_ctx* ctx, uint64_t bytes);
+/* Device bytes a count of a graph with n vertices and nnz entries needs in the workspace. */
+uint64_t ktri_workspace_bytes(uint64_t n, uint64_t nnz, int32_t intersection_method);
+const char* ktri_last_error(const ktri_ctx* ctx);
+int ktri_ctx_stats(ktri_ctx* ctx, ktri_run_stats* out); /* synchronises the context's last stream */
+const char* ktri_version(void);
+
+/* ---- counting ----------------------------------------------------------------------------- */
+/* Replaces: size_t cetric::run_shmem(DistributedGraph<>&, Statistics&, const Config&)
+ *   (include/cetric/counters/shared_memory_cetric.h:105, called from apps/shmetric.cpp:140)
+ * together with the preprocessing it runs (shared_memory_cetric.h:72-103: orient by
+ * degree_outward, distributed_graph.h:148-163 and :538-566; sort_neighborhoods, :578-593)
+ * and CetricEdgeIterator::run_local (include/cetric/counters/cetric_edge_iterator.h:173-227).
+ * Host buffers in and out; copies to and from the device are part of the call; synchronous.
+ * per_vertex_out may be NULL; otherwise it receives n counts.  opts may be NULL.
+ * Uses an internal context on the current CUDA device. */
+int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz, uint64_t* total_out,
+                   uint64_t* per_vertex_out, const ktri_opts* opts);
+
+/* Same as ktri_count_csr on an explicit context (reuses its workspace and staging). */
+int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                       uint64_t* total_out, uint64_t* per_vertex_out, const ktri_opts* opts);
+
+/* Device-resident variant, asynchronous on `stream` (a cudaStream_t, NULL = legacy default).
+ * d_first_out, d_head: device CSR.  d_total: device u64.  d_per_vertex: device u64[n] or NULL.
+ * Invalid-CSR conditions found on the device are reported by ktri_ctx_check. */
+int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n,
+                          uint64_t nnz, uint64_t* d_total, uint64_t* d_per_vertex, const ktri_opts* opts,
+                          void* stream);
+/* Synchronise the context's last stream and report device-side CSR errors of the last call. */
+int ktri_ctx_check(ktri_ctx* ctx);
+
+/* Oriented, id-sorted out-lists (the state of DistributedGraph after preprocessing,
+ * shared_memory_cetric.h:72-103, restricted to out_adj, distributed_graph.h:512-514) as a
+ * compact CSR: out_first_out[n+1] and out_head[nnz/2].  Host buffers; synchronous. */
+int ktri_orient_csr(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                    uint64_t* out_first_out, uint32_t* out_head);
+
+/* Batched set intersection of sorted u32 lists on the device, one pair per entry:
+ * pair i intersects a_vals[a_off[i]..a_off[i+1]) with b_vals[b_off[i]..b_off[i+1]) using
+ * the given strategy (cetric::intersection, intersection.h:41-79).  counts_out[i] gets the
+ * intersection size; if members_out is non-NULL it must hold a_off[npairs] entries and
+ * pair i writes its members, in increasing order, from members_out[a_off[i]].  Host buffers. */
+int ktri_intersect_pairs(ktri_ctx* ctx, int32_t method, const uint32_t* a_vals, const uint64_t* a_off,
+                         const uint32_t* b_vals, const uint64_t* b_off, uint64_t npairs, uint64_t* counts_out,
+                         uint32_t* members_out);
+
+/* ---- graphs on the host: generators and file formats ------------------------------------- */
+/* Replaces graphio::read_graph (apps/shmetric.cpp:119) and the KaGen generators behind
+ * --gen (apps/parse_parameters.h:72-73) for the inputs this engine is measured on. */
+typedef struct ktri_graph ktri_graph;
+int ktri_graph_from_csr(uint64_t n, const uint64_t* first_out, const uint32_t* head, ktri_graph** out);
+int ktri_graph_gnm(uint64_t n, uint64_t m, uint64_t seed, ktri_graph** out);
+int ktri_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                    ktri_graph** out);
+int ktri_graph_rgg2d(uint64_t n, double avg_degree, uint64_t seed, ktri_graph** out);
+int ktri_graph_read_metis(const char* path, ktri_graph** out);
+int ktri_graph_read_binary(const char* stem, ktri_graph** out);
+int ktri_graph_write_binary(const ktri_graph* g, const char* stem);
+int ktri_graph_write_metis(const ktri_graph* g, const char* path);
+uint64_t ktri_graph_n(const ktri_graph* g);
+uint64_t ktri_graph_nnz(const ktri_graph* g);
+const uint64_t* ktri_graph_first_out(const ktri_graph* g);
+const uint32_t* ktri_graph_head(const ktri_graph* g);
+void ktri_graph_free(ktri_graph* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KTRI_H */

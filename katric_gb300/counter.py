@@ -1,0 +1,235 @@
+"""Host mirror of KaTric's shared-memory counting interface, backed by the CUDA engine.
+
+  run_shmem(G, stats, conf) -> int        cetric::run_shmem (include/cetric/counters/shared_memory_cetric.h:105)
+  preprocessing(G, conf) -> (fo, head)    cetric::preprocessing (shared_memory_cetric.h:72-103): oriented,
+                                          id-sorted out-lists
+  intersection(a, b, conf) -> list        cetric::intersection (include/cetric/counters/intersection.h:41-79)
+  Config                                  the hot-path knobs of cetric::Config (include/cetric/config.h:140-200)
+  Statistics                              the counters run_shmem fills (include/cetric/statistics.h:193-217)
+
+All counting runs on the GPU through libktri.so; nothing here computes triangles on the CPU.
+Errors raise KtriError (the reference asserts or throws; the C ABI returns status codes).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from .graph import Graph
+
+METHOD_BY_NAME = {
+    "auto": _native.METHOD_AUTO,
+    "merge": _native.METHOD_MERGE,
+    "binary-search": _native.METHOD_BINARY_SEARCH,
+    "binary_search": _native.METHOD_BINARY_SEARCH,
+    "binary": _native.METHOD_BINARY,
+    "hybrid": _native.METHOD_HYBRID,
+}
+
+
+@dataclasses.dataclass
+class Config:
+    """Hot-path fields of cetric::Config with the reference's defaults (config.h:140-200).
+
+    intersection_method: "auto" (GPU default: owner-side shared-memory hash), or one of the
+    reference's "merge" (its default), "binary-search", "binary", "hybrid".  Counts are
+    identical for all five.  num_threads, pseudo2core, grainsize and the partitioning
+    switches steer CPU threading in the reference; they are accepted and recorded, and do
+    not change results.
+    """
+    intersection_method: str = "auto"
+    binary_intersection_cutoff: int = 1000
+    hybrid_cutoff_scale: float = 1.0
+    num_threads: int = 1
+    pseudo2core: bool = False
+    edge_partitioning: bool = False
+    local_degree_of_parallelism: int = 1
+    high_degree_threshold_scale: float = 1.0
+    iterations: int = 1
+    per_vertex: bool = True
+    collect_stats: bool = False
+    device: int = 0
+
+    def opts(self) -> _native.Opts:
+        o = _native.Opts()
+        o.struct_size = ctypes.sizeof(_native.Opts)
+        try:
+            o.intersection_method = METHOD_BY_NAME[self.intersection_method.lower()]
+        except KeyError:
+            raise ValueError(f"unknown intersection method {self.intersection_method!r}") from None
+        o.small_outdegree = 0
+        o.collect_stats = 1 if self.collect_stats else 0
+        o.binary_intersection_cutoff = self.binary_intersection_cutoff
+        o.hybrid_cutoff_scale = self.hybrid_cutoff_scale
+        return o
+
+
+@dataclasses.dataclass
+class LocalStatistics:
+    local_triangles: int = 0
+    wedge_checks: int = 0
+    intersection_size_local: int = 0
+    oriented_edges: int = 0
+    streamed_entries: int = 0
+    input_sorted: bool = True
+    local_phase_time: float = 0.0   # seconds, device time of intersection + reduction
+    preprocessing_time: float = 0.0  # seconds, device time of orientation (+ sort)
+    wedges: int = 0
+
+
+@dataclasses.dataclass
+class Statistics:
+    """Filled by run_shmem: counted_triangles, per-vertex counts and phase timers."""
+    local: LocalStatistics = dataclasses.field(default_factory=LocalStatistics)
+    counted_triangles: int = 0
+    per_vertex: Optional[np.ndarray] = None
+    global_wall_time: float = 0.0
+
+
+class TriangleCounter:
+    """One library context on one GPU: owns the device workspace across calls."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 0):
+        self._L = _native.load()
+        h = ctypes.c_void_p()
+        _native.check(self._L.ktri_ctx_create(device, ctypes.byref(h)))
+        self._ctx = h
+        self.device = device
+        if memory_budget:
+            self.set_memory_budget(memory_budget)
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None) is not None:
+            self._L.ktri_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    def set_memory_budget(self, nbytes: int) -> None:
+        _native.check(self._L.ktri_ctx_set_memory_budget(self._ctx, nbytes), self._ctx)
+
+    def _check(self, rc: int) -> None:
+        _native.check(rc, self._ctx)
+
+    def count(self, first_out, head, conf: Config | None = None, per_vertex: bool = True):
+        """Host CSR in, (total, per-vertex counts or None) out; copies are part of the call."""
+        conf = conf or Config()
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, nnz = len(fo) - 1, len(hd)
+        total = ctypes.c_uint64(0)
+        pv = np.zeros(max(n, 1), dtype=np.uint64) if per_vertex else None
+        opts = conf.opts()
+        self._check(self._L.ktri_count_csr_ctx(self._ctx, fo.ctypes.data, hd.ctypes.data if nnz else None, n, nnz,
+                                               ctypes.byref(total), pv.ctypes.data if pv is not None else None,
+                                               ctypes.byref(opts)))
+        return int(total.value), (pv[:n] if pv is not None else None)
+
+    def count_device(self, first_out_ptr: int, head_ptr: int, n: int, nnz: int, total_ptr: int,
+                     per_vertex_ptr: int | None = None, conf: Config | None = None, stream: int = 0) -> None:
+        """Device CSR in, device outputs; asynchronous on `stream` (a cudaStream_t as int)."""
+        conf = conf or Config()
+        opts = conf.opts()
+        self._check(self._L.ktri_count_csr_device(self._ctx, first_out_ptr, head_ptr, n, nnz, total_ptr,
+                                                  per_vertex_ptr, ctypes.byref(opts), stream or None))
+
+    def check(self) -> None:
+        self._check(self._L.ktri_ctx_check(self._ctx))
+
+    def stats(self) -> _native.RunStats:
+        st = _native.RunStats()
+        self._check(self._L.ktri_ctx_stats(self._ctx, ctypes.byref(st)))
+        return st
+
+    def orient(self, first_out, head):
+        """Oriented, id-sorted out-lists as a compact CSR (u64 offsets, u32 ids)."""
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, nnz = len(fo) - 1, len(hd)
+        ofo = np.zeros(n + 1, dtype=np.uint64)
+        oh = np.zeros(max(1, nnz // 2 + 1), dtype=np.uint32)
+        self._check(self._L.ktri_orient_csr(self._ctx, fo.ctypes.data, hd.ctypes.data if nnz else None, n, nnz,
+                                            ofo.ctypes.data, oh.ctypes.data))
+        return ofo, oh[: int(ofo[-1])].copy()
+
+    def intersect_pairs(self, pairs, method: str = "merge", members: bool = True):
+        """Intersect each (a, b) pair of sorted u32 lists on the device.
+
+        Returns a list of intersections (lists) when members is true, else the sizes."""
+        a_lists = [np.ascontiguousarray(a, dtype=np.uint32) for a, _ in pairs]
+        b_lists = [np.ascontiguousarray(b, dtype=np.uint32) for _, b in pairs]
+        a_off = np.zeros(len(pairs) + 1, dtype=np.uint64)
+        b_off = np.zeros(len(pairs) + 1, dtype=np.uint64)
+        a_off[1:] = np.cumsum([len(a) for a in a_lists]) if pairs else []
+        b_off[1:] = np.cumsum([len(b) for b in b_lists]) if pairs else []
+        av = np.concatenate(a_lists) if a_lists and a_off[-1] else np.zeros(1, np.uint32)
+        bv = np.concatenate(b_lists) if b_lists and b_off[-1] else np.zeros(1, np.uint32)
+        counts = np.zeros(max(1, len(pairs)), dtype=np.uint64)
+        mem = np.zeros(max(1, int(a_off[-1])), dtype=np.uint32) if members else None
+        self._check(self._L.ktri_intersect_pairs(self._ctx, METHOD_BY_NAME[method], av.ctypes.data,
+                                                 a_off.ctypes.data, bv.ctypes.data, b_off.ctypes.data, len(pairs),
+                                                 counts.ctypes.data, mem.ctypes.data if mem is not None else None))
+        if not members:
+            return [int(c) for c in counts[: len(pairs)]]
+        return [[int(x) for x in mem[int(a_off[i]): int(a_off[i]) + int(counts[i])]] for i in range(len(pairs))]
+
+
+_default: dict[int, TriangleCounter] = {}
+
+
+def default_counter(device: int = 0) -> TriangleCounter:
+    if device not in _default:
+        _default[device] = TriangleCounter(device)
+    return _default[device]
+
+
+def run_shmem(G: Graph, stats: Statistics, conf: Config) -> int:
+    """cetric::run_shmem: orientation + sort + local phase on G; returns the triangle count.
+
+    Unlike the reference, G is not modified (the engine orients a device copy); the
+    per-vertex counts are left in stats.per_vertex."""
+    ctr = default_counter(conf.device)
+    c2 = dataclasses.replace(conf, collect_stats=conf.collect_stats)
+    total, pv = ctr.count(G.first_out, G.head, c2, per_vertex=conf.per_vertex)
+    st = ctr.stats()
+    stats.counted_triangles = total
+    stats.per_vertex = pv
+    stats.local.local_triangles = total
+    stats.local.wedge_checks = int(st.wedge_checks)
+    stats.local.intersection_size_local = int(st.intersection_size_local)
+    stats.local.oriented_edges = int(st.oriented_edges)
+    stats.local.streamed_entries = int(st.streamed_entries)
+    stats.local.input_sorted = bool(st.input_sorted)
+    stats.local.preprocessing_time = st.ms_orient / 1e3
+    stats.local.local_phase_time = st.ms_count / 1e3
+    stats.global_wall_time = st.ms_total / 1e3
+    return total
+
+
+def preprocessing(G: Graph, conf: Config | None = None):
+    """Oriented out-lists after orient(degree_outward) + sort_neighborhoods(id), as a compact CSR."""
+    return default_counter((conf or Config()).device).orient(G.first_out, G.head)
+
+
+def intersection(a, b, conf: Config | None = None) -> list[int]:
+    """cetric::intersection of two sorted lists with conf.intersection_method, on the device."""
+    conf = conf or Config(intersection_method="merge")
+    return default_counter(conf.device).intersect_pairs([(a, b)], method=conf.intersection_method)[0]

@@ -1,0 +1,544 @@
+// C ABI: contexts, workspace management and the counting entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ktri.h"
+#include "ktri_device.cuh"
+#include "ktri_internal.h"
+#include "ktri_kernels.h"
+
+using ktri::Control;
+using ktri::u32;
+using ktri::u64;
+
+struct ktri_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;  // stream of the host-buffer entry points
+    void* ws = nullptr;             // grow-only device workspace
+    size_t ws_bytes = 0;
+    uint64_t budget = 0;
+    std::string last_error;
+    ktri_run_stats stats{};
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t last_stream = nullptr;
+    Control* ctl = nullptr;
+    bool pending = false;      // a device call whose status has not been read yet
+    bool have_events = false;
+    int32_t last_method = KTRI_METHOD_AUTO;
+    bool last_collect = false;
+};
+
+namespace {
+
+constexpr size_t ALIGN = 256;
+inline size_t align_up(size_t x) { return (x + ALIGN - 1) & ~(ALIGN - 1); }
+
+struct Layout {
+    size_t ctl = 0, deg = 0, dplus = 0, vdesc = 0, headp = 0, ltiles = 0, spanning = 0, partials = 0, cnt = 0,
+           total = 0, mid = 0, big = 0, scratch = 0, in_fo = 0, in_head = 0, bytes = 0;
+    bool wide = false;
+    u64 scratch_per_block = 0;
+    int big_grid = 0;
+    u32 npartials = 0;
+};
+
+u64 isqrt_ceil(u64 x) {
+    u64 r = (u64)std::sqrt((double)x);
+    while (r * r < x) ++r;
+    while (r > 0 && (r - 1) * (r - 1) >= x) --r;
+    return r;
+}
+
+// Workspace of one count.  num_sms = 0 sizes the grids for the largest supported part.
+Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs, bool internal_cnt) {
+    Layout L;
+    const u64 cap = ktri::oriented_capacity(n, nnz);
+    L.wide = cap > 0xFFFFFFFFull;
+    const int sms = num_sms > 0 ? num_sms : 160;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes);
+        return at;
+    };
+    L.ctl = take(sizeof(Control));
+    L.deg = take(sizeof(u32) * (n + 1));
+    L.dplus = take(sizeof(u32) * (n + 1));
+    L.vdesc = take((L.wide ? 16 : 8) * (n + 1));
+    L.headp = take(sizeof(u32) * cap);
+    L.spanning = take(sizeof(u32) * ktri::spanning_capacity(n, nnz));
+    u32 grid = 0;
+    if (method == KTRI_METHOD_AUTO) {
+        L.ltiles = take(sizeof(uint2) * ktri::large_tile_capacity(n, nnz, ktri::SMALL_D));
+        grid = (u32)(sms * 16);  // bound on small + large persistent grids (occupancy <= 8 each)
+    } else {
+        L.mid = take(sizeof(u32) * (n + 1));
+        L.big = take(sizeof(u32) * (n + 1));
+        u64 maxd = isqrt_ceil(nnz) + 1;
+        u64 P = 1;
+        while (P < maxd) P <<= 1;
+        L.scratch_per_block = P;
+        L.big_grid = sms;
+        L.scratch = take(sizeof(u32) * P * (u64)sms);
+        grid = (u32)ktri::count_grid_edges(sms);
+    }
+    L.npartials = grid;
+    L.partials = take(sizeof(u64) * grid);
+    if (internal_cnt) L.cnt = take(sizeof(u64) * (n + 1));
+    L.total = take(sizeof(u64));
+    if (with_inputs) {
+        L.in_fo = take(sizeof(u64) * (n + 1));
+        L.in_head = take(sizeof(u32) * (nnz + 1));
+    }
+    L.bytes = off;
+    return L;
+}
+
+int set_error(ktri_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int cuda_fail(ktri_ctx* ctx, cudaError_t e, const char* what) {
+    return set_error(ctx, e == cudaErrorMemoryAllocation ? KTRI_ERR_OUT_OF_MEMORY : KTRI_ERR_CUDA,
+                     std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define KTRI_CK(ctx, call)                                       \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+ktri::Options resolve(const ktri_opts* o) {
+    ktri::Options r;
+    if (!o || o->struct_size == 0) return r;
+    r.method = o->intersection_method;
+    if (o->small_outdegree) r.small_outdegree = o->small_outdegree;
+    r.collect_stats = o->collect_stats != 0;
+    if (o->binary_intersection_cutoff) r.binary_cutoff = o->binary_intersection_cutoff;
+    if (o->hybrid_cutoff_scale > 0) r.hybrid_scale = o->hybrid_cutoff_scale;
+    return r;
+}
+
+int ensure_ws(ktri_ctx* ctx, size_t bytes) {
+    if (ctx->budget && bytes > ctx->budget)
+        return set_error(ctx, KTRI_ERR_OUT_OF_MEMORY,
+                         "workspace of " + std::to_string(bytes) + " bytes exceeds the memory budget of " +
+                             std::to_string(ctx->budget));
+    if (bytes <= ctx->ws_bytes) return KTRI_OK;
+    if (ctx->ws) {
+        KTRI_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+        cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+        ctx->ws_bytes = 0;
+    }
+    size_t grow = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&ctx->ws, grow);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaMalloc(&ctx->ws, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ctx->ws = nullptr;
+            return cuda_fail(ctx, e, "cudaMalloc(workspace)");
+        }
+        grow = bytes;
+    }
+    ctx->ws_bytes = grow;
+    return KTRI_OK;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <typename OffT>
+int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total,
+                 u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all) {
+    char* base = static_cast<char*>(ctx->ws);
+    auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
+    auto* deg = reinterpret_cast<u32*>(base + L.deg);
+    auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
+    void* vdesc = base + L.vdesc;
+    auto* headp = reinterpret_cast<u32*>(base + L.headp);
+    auto* spanning = reinterpret_cast<u32*>(base + L.spanning);
+    auto* partials = reinterpret_cast<u64*>(base + L.partials);
+    const int sms = ctx->num_sms;
+
+    KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
+    ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, ctl, sms, st);
+    ktri::launch_orient(fo, head, n, nnz, deg, headp, dplus, spanning, ctl, st);
+    const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
+    auto* ltiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, ltiles, autom ? (u32)ktri::SMALL_D : 0xFFFFFFFFu,
+                            ktri::LARGE_SEG, ctl, sms, st);
+    if (!autom) {
+        ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
+                                      reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
+                                      L.scratch_per_block, L.big_grid, ctl, sms, st);
+    }
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev[1], st));
+    if (opt.collect_stats) ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, ctl, sms, st);
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
+    if (sort_all) {
+        // orientation export only: no counting
+    } else if (autom) {
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, ltiles, cnt, partials, ctl, sms, st,
+                                                   ctx->ev[4], ctx->ev[5]));
+        const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
+        ktri::launch_final(partials, np, d_total, ctl, st);
+    } else {
+        const int grid = ktri::count_grid_edges(sms);
+        ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
+                                       grid, ctl, st);
+        ktri::launch_final(partials, (u32)grid, d_total, ctl, st);
+    }
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev[3], st));
+    KTRI_CK(ctx, cudaGetLastError());
+    ctx->ctl = ctl;
+    ctx->last_stream = st;
+    ctx->pending = true;
+    ctx->have_events = true;
+    ctx->last_method = opt.method;
+    ctx->last_collect = opt.collect_stats;
+    ctx->stats = ktri_run_stats{};
+    ctx->stats.n = n;
+    ctx->stats.nnz = nnz;
+    ctx->stats.method = (u32)opt.method;
+    return KTRI_OK;
+}
+
+int check_common(ktri_ctx* ctx, const void* fo, const void* head, u64 n, u64 nnz, const void* total,
+                 const ktri::Options& opt) {
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!total) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "total output pointer is NULL");
+    if (n > 0xFFFFFFFFull) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "n must be below 2^32 (u32 vertex ids)");
+    if (n && !fo) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "first_out is NULL");
+    if (nnz && !head) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "head is NULL");
+    if (n == 0 && nnz != 0) return set_error(ctx, KTRI_ERR_INVALID_CSR, "nnz > 0 with n == 0");
+    if (opt.method < KTRI_METHOD_AUTO || opt.method > KTRI_METHOD_HYBRID)
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "unknown intersection method");
+    if (opt.method == KTRI_METHOD_AUTO && opt.small_outdegree != (u32)ktri::SMALL_D)
+        return set_error(ctx, KTRI_ERR_UNSUPPORTED, "small_outdegree other than 32 is not built in");
+    return KTRI_OK;
+}
+
+int device_status(ktri_ctx* ctx) {
+    if (!ctx->pending) return KTRI_OK;
+    KTRI_CK(ctx, cudaStreamSynchronize(ctx->last_stream));
+    Control h;
+    KTRI_CK(ctx, cudaMemcpy(&h, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    ctx->pending = false;
+    ctx->stats.input_sorted = (h.err & ktri::DEV_FLAG_UNSORTED) ? 0 : 1;
+    if (ctx->last_collect) {
+        ctx->stats.wedge_checks = h.stat_wedge;
+        ctx->stats.intersection_size_local = h.stat_isz;
+        ctx->stats.streamed_entries = h.stat_streamed;
+        ctx->stats.oriented_edges = h.stat_oriented;
+    }
+    if (ctx->have_events) {
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&b, ctx->ev[2], ctx->ev[3]);
+        cudaEventElapsedTime(&c, ctx->ev[0], ctx->ev[3]);
+        ctx->stats.ms_orient = a;
+        ctx->stats.ms_count = b;
+        ctx->stats.ms_total = c;
+        if (ctx->last_method == KTRI_METHOD_AUTO) {
+            float s1 = 0, s2 = 0;
+            cudaEventElapsedTime(&s1, ctx->ev[2], ctx->ev[4]);
+            cudaEventElapsedTime(&s2, ctx->ev[4], ctx->ev[5]);
+            ctx->stats.ms_count_small = s1;
+            ctx->stats.ms_count_large = s2;
+        }
+    }
+    const u32 e = h.err & ktri::DEV_ERR_MASK;
+    if (e & ktri::DEV_ERR_DEGREE)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out is not a valid offset array (non-monotone, "
+                                                    "first_out[0] != 0, first_out[n] != nnz, or a degree >= 2^32)");
+    if (e & ktri::DEV_ERR_ID_RANGE) return set_error(ctx, KTRI_ERR_INVALID_CSR, "adjacency entry >= n");
+    if (e & ktri::DEV_ERR_SELF_LOOP) return set_error(ctx, KTRI_ERR_INVALID_CSR, "self-loop in the adjacency");
+    if (e & ktri::DEV_ERR_DUPLICATE) return set_error(ctx, KTRI_ERR_INVALID_CSR, "duplicate adjacency entry");
+    return KTRI_OK;
+}
+
+std::mutex g_default_mu;
+std::map<int, ktri_ctx*> g_default;
+
+}  // namespace
+
+extern "C" {
+
+const char* ktri_version(void) { return "katric_gb300 1.0 (sm_103a)"; }
+
+int ktri_ctx_create(int device, ktri_ctx** out) {
+    if (!out) return KTRI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return KTRI_ERR_NO_DEVICE;
+    }
+    if (device < 0) cudaGetDevice(&device);
+    if (device >= ndev) return KTRI_ERR_NO_DEVICE;
+    ktri_ctx* ctx = new (std::nothrow) ktri_ctx();
+    if (!ctx) return KTRI_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    DeviceGuard g(device);
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return KTRI_ERR_CUDA;
+    }
+    for (auto& e : ctx->ev) cudaEventCreate(&e);
+    *out = ctx;
+    return KTRI_OK;
+}
+
+int ktri_ctx_destroy(ktri_ctx* ctx) {
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    {
+        DeviceGuard g(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        if (ctx->last_stream && ctx->last_stream != ctx->stream) cudaStreamSynchronize(ctx->last_stream);
+        if (ctx->ws) cudaFree(ctx->ws);
+        for (auto& e : ctx->ev)
+            if (e) cudaEventDestroy(e);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return KTRI_OK;
+}
+
+int ktri_ctx_set_memory_budget(ktri_ctx* ctx, uint64_t bytes) {
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    ctx->budget = bytes;
+    return KTRI_OK;
+}
+
+uint64_t ktri_workspace_bytes(uint64_t n, uint64_t nnz, int32_t method) {
+    return make_layout(n, nnz, method, 0, false, true).bytes;
+}
+
+const char* ktri_last_error(const ktri_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int ktri_ctx_stats(ktri_ctx* ctx, ktri_run_stats* out) {
+    if (!ctx || !out) return KTRI_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(ctx->device);
+    int rc = device_status(ctx);
+    *out = ctx->stats;
+    return rc;
+}
+
+int ktri_ctx_check(ktri_ctx* ctx) {
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(ctx->device);
+    return device_status(ctx);
+}
+
+int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n,
+                          uint64_t nnz, uint64_t* d_total, uint64_t* d_per_vertex, const ktri_opts* opts,
+                          void* stream) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_common(ctx, d_first_out, d_head, n, nnz, d_total, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) {
+        rc = device_status(ctx);
+        (void)rc;  // the previous call's status was not collected; the new call proceeds
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        KTRI_CK(ctx, cudaMemsetAsync(d_total, 0, sizeof(u64), st));
+        ctx->pending = false;
+        ctx->stats = ktri_run_stats{};
+        return KTRI_OK;
+    }
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, false, d_per_vertex == nullptr);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex)
+                            : reinterpret_cast<u64*>(static_cast<char*>(ctx->ws) + L.cnt);
+    auto* fo = reinterpret_cast<const u64*>(d_first_out);
+    auto* tot = reinterpret_cast<u64*>(d_total);
+    if (L.wide) return run_pipeline<u64>(ctx, L, fo, d_head, n, nnz, tot, cnt, opt, st, false);
+    return run_pipeline<u32>(ctx, L, fo, d_head, n, nnz, tot, cnt, opt, st, false);
+}
+
+int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                       uint64_t* total_out, uint64_t* per_vertex_out, const ktri_opts* opts) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_common(ctx, first_out, head, n, nnz, total_out, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    if (n == 0) {
+        *total_out = 0;
+        return KTRI_OK;
+    }
+    if (first_out[0] != 0 || first_out[n] != nnz)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz, cudaMemcpyHostToDevice, st));
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false);
+    if (rc) return rc;
+    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
+    if (per_vertex_out)
+        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
+    return rc;
+}
+
+int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz, uint64_t* total_out,
+                   uint64_t* per_vertex_out, const ktri_opts* opts) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return KTRI_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    ktri_ctx*& ctx = g_default[dev];
+    if (!ctx) {
+        int rc = ktri_ctx_create(dev, &ctx);
+        if (rc) {
+            ctx = nullptr;
+            return rc;
+        }
+    }
+    return ktri_count_csr_ctx(ctx, first_out, head, n, nnz, total_out, per_vertex_out, opts);
+}
+
+int ktri_orient_csr(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                    uint64_t* out_first_out, uint32_t* out_head) {
+    if (!ctx || !out_first_out || (n && !first_out) || (nnz && (!head || !out_head)))
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "null pointer");
+    if (n > 0xFFFFFFFFull) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "n must be below 2^32");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    out_first_out[0] = 0;
+    if (n == 0) return KTRI_OK;
+    if (first_out[0] != 0 || first_out[n] != nnz)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
+    ktri::Options opt;
+    opt.method = KTRI_METHOD_MERGE;
+    Layout L = make_layout(n, nnz, KTRI_METHOD_MERGE, ctx->num_sms, true, true);
+    // room for the exported CSR: out offsets (u64[n+1]) and out heads (u32[nnz/2])
+    const size_t off_ofo = L.bytes, off_oh = align_up(off_ofo + sizeof(u64) * (n + 1));
+    const size_t total_bytes = align_up(off_oh + sizeof(u32) * (nnz / 2 + 1));
+    int rc = ensure_ws(ctx, total_bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_ofo = reinterpret_cast<u64*>(base + off_ofo);
+    auto* d_oh = reinterpret_cast<u32*>(base + off_oh);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz, cudaMemcpyHostToDevice, st));
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, true)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, true);
+    if (rc) return rc;
+    if (L.wide) ktri::launch_outdeg<u64>(n, base + L.vdesc, d_cnt, ctx->num_sms, st);
+    else ktri::launch_outdeg<u32>(n, base + L.vdesc, d_cnt, ctx->num_sms, st);
+    std::vector<u64> outdeg(n);
+    KTRI_CK(ctx, cudaMemcpyAsync(outdeg.data(), d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc) return rc;
+    for (u64 v = 0; v < n; ++v) out_first_out[v + 1] = out_first_out[v] + outdeg[v];
+    if (out_first_out[n] > nnz / 2 + 1) return set_error(ctx, KTRI_ERR_INVALID_CSR, "graph is not symmetric");
+    KTRI_CK(ctx, cudaMemcpyAsync(d_ofo, out_first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (L.wide) ktri::launch_export<u64>(n, base + L.vdesc, reinterpret_cast<u32*>(base + L.headp), d_ofo, d_oh,
+                                         ctx->num_sms, st);
+    else ktri::launch_export<u32>(n, base + L.vdesc, reinterpret_cast<u32*>(base + L.headp), d_ofo, d_oh,
+                                  ctx->num_sms, st);
+    if (out_first_out[n])
+        KTRI_CK(ctx, cudaMemcpyAsync(out_head, d_oh, sizeof(u32) * out_first_out[n], cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaStreamSynchronize(st));
+    KTRI_CK(ctx, cudaGetLastError());
+    return KTRI_OK;
+}
+
+int ktri_intersect_pairs(ktri_ctx* ctx, int32_t method, const uint32_t* a_vals, const uint64_t* a_off,
+                         const uint32_t* b_vals, const uint64_t* b_off, uint64_t npairs, uint64_t* counts_out,
+                         uint32_t* members_out) {
+    if (!ctx || !a_off || !b_off || !counts_out) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "null pointer");
+    if (method < KTRI_METHOD_AUTO || method > KTRI_METHOD_HYBRID)
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "unknown intersection method");
+    if (npairs == 0) return KTRI_OK;
+    const u64 na = a_off[npairs], nb = b_off[npairs];
+    for (u64 i = 0; i < npairs; ++i) {
+        if (a_off[i + 1] < a_off[i] || b_off[i + 1] < b_off[i] || a_off[i + 1] - a_off[i] > 0xFFFFFFFFull ||
+            b_off[i + 1] - b_off[i] > 0xFFFFFFFFull)
+            return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
+    }
+    if ((na && !a_vals) || (nb && !b_vals)) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "null list values");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes);
+        return at;
+    };
+    const size_t o_av = take(4 * (na + 1)), o_bv = take(4 * (nb + 1)), o_ao = take(8 * (npairs + 1)),
+                 o_bo = take(8 * (npairs + 1)), o_c = take(8 * npairs), o_m = take(4 * (na + 1)), o_e = take(4);
+    int rc = ensure_ws(ctx, off);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    cudaStream_t st = ctx->stream;
+    if (na) KTRI_CK(ctx, cudaMemcpyAsync(base + o_av, a_vals, 4 * na, cudaMemcpyHostToDevice, st));
+    if (nb) KTRI_CK(ctx, cudaMemcpyAsync(base + o_bv, b_vals, 4 * nb, cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(base + o_ao, a_off, 8 * (npairs + 1), cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(base + o_bo, b_off, 8 * (npairs + 1), cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, cudaMemsetAsync(base + o_e, 0, 4, st));
+    ktri::launch_intersect_pairs(method, reinterpret_cast<u32*>(base + o_av), reinterpret_cast<u64*>(base + o_ao),
+                                 reinterpret_cast<u32*>(base + o_bv), reinterpret_cast<u64*>(base + o_bo), npairs,
+                                 1000, 1.0, reinterpret_cast<u64*>(base + o_c),
+                                 members_out ? reinterpret_cast<u32*>(base + o_m) : nullptr,
+                                 reinterpret_cast<int*>(base + o_e), st);
+    KTRI_CK(ctx, cudaGetLastError());
+    KTRI_CK(ctx, cudaMemcpyAsync(counts_out, base + o_c, 8 * npairs, cudaMemcpyDeviceToHost, st));
+    if (members_out && na) KTRI_CK(ctx, cudaMemcpyAsync(members_out, base + o_m, 4 * na, cudaMemcpyDeviceToHost, st));
+    int herr = 0;
+    KTRI_CK(ctx, cudaMemcpyAsync(&herr, base + o_e, 4, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaStreamSynchronize(st));
+    if (herr) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "binary intersection stack overflow");
+    return KTRI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,532 @@
+// Owner-side hash counting (KTRI_METHOD_AUTO): the GPU form of CetricEdgeIterator::run_local
+// (cetric_edge_iterator.h:889-1066) with intersection() (intersection.h:41-79).
+//
+// Every undirected edge {x,y} contributes |N+(x) ∩ N+(y)| triangles, where N+ is the
+// out-list after orientation by (degree, id); the sum over all edges is the triangle total,
+// exactly as the reference's sum over oriented edges (v,u) of |N+(v) ∩ N+(u)|.  The edge is
+// evaluated once, at its "owner": the endpoint whose (out-degree, id) is larger.  The owner's
+// out-list sits in a shared-memory hash table and the other endpoint's (shorter) out-list
+// is streamed through it, so the work of an edge is min(|N+(x)|, |N+(y)|) probes.
+//
+// Per-vertex counts: a hit w of edge {x,y} is the triangle {x,y,w}.  w is a key of the
+// owner's table: its hits accumulate in a shared-memory counter next to the key and are
+// flushed once per table.  y gets one atomic per edge, x one per tile.
+//
+// Two kernels split the owners by out-degree:
+//   k_count_small: owners with out-degree <= SMALL_D.  Merge-path tiles over the adjacency
+//     (as in orientation) give every block the same number of slots; the tables of all
+//     owners in a tile live side by side in shared memory.
+//   k_count_large: owners above SMALL_D, one (owner, segment of LARGE_SEG slots) tile per
+//     block iteration; long streamed lists are shared out to whole warps.
+#include "ktri_device.cuh"
+#include "ktri_kernels.h"
+
+namespace ktri {
+
+template <int BLOCK, int IPT, int SD, typename OffT>
+struct SmallLayout {
+    static constexpr int TILE = BLOCK * IPT;
+    static constexpr int TBL = 4 * (TILE + 2 * SD);  // sum of per-owner table sizes (pow2 >= 2 d <= 4 d)
+    static constexpr int WPT = (TILE + 1 + BLOCK - 1) / BLOCK;
+    static constexpr size_t off_fo = 0;
+    static constexpr size_t off_desc = off_fo + sizeof(u64) * (TILE + 2);
+    static constexpr size_t off_head = off_desc + sizeof(Desc<OffT>) * (TILE + 2);
+    static constexpr size_t off_tb = off_head + sizeof(u32) * TILE;
+    static constexpr size_t off_ko = off_tb + sizeof(u32) * (TILE + 2);
+    static constexpr size_t off_own = off_ko + sizeof(u32) * (TILE + 2);
+    static constexpr size_t off_keys = off_own + sizeof(u32) * (TILE + 2);
+    static constexpr size_t off_hits = off_keys + sizeof(u32) * TBL;
+    static constexpr size_t bytes = off_hits + sizeof(u32) * TBL;
+};
+
+template <int BLOCK, int IPT, int SD, typename OffT>
+__global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
+                                                       u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
+                                                       const u32* __restrict__ headp, u64* __restrict__ cnt,
+                                                       u64* __restrict__ partials, Control* ctl) {
+    using L = SmallLayout<BLOCK, IPT, SD, OffT>;
+    constexpr int TILE = L::TILE;
+    constexpr int WPT = L::WPT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* s_fo = reinterpret_cast<u64*>(smem + L::off_fo);
+    Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
+    u32* s_head = reinterpret_cast<u32*>(smem + L::off_head);
+    u32* s_tb = reinterpret_cast<u32*>(smem + L::off_tb);
+    u32* s_ko = reinterpret_cast<u32*>(smem + L::off_ko);
+    u32* s_own = reinterpret_cast<u32*>(smem + L::off_own);
+    u32* s_keys = reinterpret_cast<u32*>(smem + L::off_keys);
+    u32* s_hits = reinterpret_cast<u32*>(smem + L::off_hits);
+    __shared__ u32 s_warp[BLOCK / 32];
+    __shared__ u64 s_red[BLOCK / 32];
+    __shared__ u64 s_b[3];
+
+    if (ctl->err & DEV_ERR_MASK) return;
+    const u64 total_items = n + nnz;
+    const u64 ntiles = (total_items + TILE - 1) / TILE;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    u64 local_total = 0;
+    u32 dup = 0;
+
+    while (true) {
+        if (threadIdx.x == 0) s_b[2] = atomicAdd(&ctl->small_next, 1ull);
+        __syncthreads();
+        const u64 tile = s_b[2];
+        if (tile >= ntiles) break;
+        const u64 d0 = tile * TILE;
+        const u64 d1 = d0 + TILE < total_items ? d0 + TILE : total_items;
+        if (threadIdx.x == 0) s_b[0] = mp_search(fo, n, d0);
+        if (threadIdx.x == 32) s_b[1] = mp_search(fo, n, d1);
+        __syncthreads();
+        const u64 i0 = s_b[0], i1 = s_b[1];
+        if (i0 >= n) {  // only trailing vertex-end events: nothing to count
+            __syncthreads();
+            continue;
+        }
+        const u64 j0 = d0 - i0, j1 = d1 - i1;
+        const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
+        const u32 nw = (u32)(fo_last - i0);  // window vertices [i0, fo_last)
+        for (u32 k = threadIdx.x; k <= nw; k += BLOCK) s_fo[k] = fo[i0 + k];
+        for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
+            s_desc[k] = load_desc(vdesc + i0 + k);
+            s_own[k] = 0;
+        }
+        const u32 nslot = (u32)(j1 - j0);
+        for (u32 k = threadIdx.x; k < nslot; k += BLOCK) s_head[k] = head[j0 + k];
+        __syncthreads();
+
+        // table sizes and key offsets of the owners in the window
+        u32 packed[WPT];
+        u32 tsum = 0;
+#pragma unroll
+        for (int r = 0; r < WPT; ++r) {
+            const u32 k = threadIdx.x * WPT + r;
+            packed[r] = 0;
+            if (k < nw) {
+                const u64 a = s_fo[k], b = s_fo[k + 1];
+                const u64 lo = a > j0 ? a : j0, hi = b < j1 ? b : j1;
+                const u32 d = s_desc[k].d;
+                if (lo < hi && d > 0 && d <= (u32)SD) {
+                    u32 lg = ceil_log2(2 * d);
+                    if (lg < 1) lg = 1;
+                    packed[r] = ((1u << lg) << 16) | d;
+                }
+            }
+            tsum += packed[r];
+        }
+        u32 ptot;
+        u32 pbase = block_exclusive_scan<BLOCK>(tsum, s_warp, &ptot);
+#pragma unroll
+        for (int r = 0; r < WPT; ++r) {
+            const u32 k = threadIdx.x * WPT + r;
+            if (k < nw) {
+                const u32 p = packed[r];
+                if (p) {
+                    const u32 sz = p >> 16;
+                    s_tb[k] = ((pbase >> 16) << 5) | (31 - __clz(sz));
+                } else {
+                    s_tb[k] = NONE;
+                }
+                s_ko[k] = pbase & 0xFFFFu;
+            }
+            pbase += packed[r];
+        }
+        const u32 table_slots = ptot >> 16, nkeys = ptot & 0xFFFFu;
+        if (threadIdx.x == 0) s_ko[nw] = nkeys;
+        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
+            s_keys[s] = EMPTY_KEY;
+            s_hits[s] = 0;
+        }
+        __syncthreads();
+
+        // insert the out-lists of the owners (one key per thread per step)
+        for (u32 q = threadIdx.x; q < nkeys; q += BLOCK) {
+            u32 lo = 0, hi = nw - 1;
+            while (lo < hi) {
+                u32 mid = (lo + hi + 1) >> 1;
+                if (s_ko[mid] <= q) lo = mid; else hi = mid - 1;
+            }
+            const u32 tb = s_tb[lo];
+            const u32 w = __ldg(headp + (u64)s_desc[lo].start + (q - s_ko[lo]));
+            if (!table_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
+        }
+        __syncthreads();
+
+        // walk this thread's items of the merge path
+        const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
+        const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
+        const u64 i_start = mp_search_window(s_fo, i0, i0, i1 < fo_last ? i1 : fo_last, dt);
+        u32 own[IPT], yv[IPT];
+        {
+            u64 i = i_start, j = dt - i_start;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                own[k] = NONE;
+                yv[k] = 0;
+                if (dt + k < dte) {
+                    if (i < n && j < s_fo[i + 1 - i0]) {
+                        const u32 o = (u32)(i - i0);
+                        if (s_tb[o] != NONE) {
+                            own[k] = o;
+                            yv[k] = s_head[j - j0];
+                        }
+                        ++j;
+                    } else {
+                        ++i;
+                    }
+                }
+            }
+        }
+        Desc<OffT> vy[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            vy[k].start = 0;
+            vy[k].d = 0;
+            if (own[k] != NONE && yv[k] < n) vy[k] = load_desc(vdesc + yv[k]);
+        }
+        u32 run_owner = NONE, run = 0;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const u32 o = own[k];
+            if (o == NONE) continue;
+            const u32 dx = s_desc[o].d;
+            const u32 y = yv[k];
+            const u32 dy = vy[k].d;
+            u32 hits = 0;
+            if (dy > 0 && key_less(dy, y, dx, i0 + o)) {
+                const u32 tb = s_tb[o];
+                u32* keys = s_keys + (tb >> 5);
+                u32* hitc = s_hits + (tb >> 5);
+                const u32 lg = tb & 31u;
+                const u64 q0 = (u64)vy[k].start >> 2;
+#pragma unroll
+                for (int c = 0; c < SD / 4; ++c) {
+                    if (4 * c < (int)dy) {
+                        const uint4 q = __ldg(headp4 + q0 + c);
+                        const u32 wv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            if (4 * c + e < (int)dy) {
+                                const u32 s = table_find(keys, lg, wv[e]);
+                                if (s != NONE) {
+                                    atomicAdd(&hitc[s], 1u);
+                                    ++hits;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            if (hits) atomicAdd(&cnt[y], (u64)hits);
+            if (o != run_owner) {
+                if (run) atomicAdd(&s_own[run_owner], run);
+                run_owner = o;
+                run = 0;
+            }
+            run += hits;
+        }
+        if (run) atomicAdd(&s_own[run_owner], run);
+        __syncthreads();
+
+        // flush: hits of every key (vertex w), then the owners' own counts
+        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
+            const u32 h = s_hits[s];
+            if (h) atomicAdd(&cnt[s_keys[s]], (u64)h);
+        }
+        for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
+            const u32 t = s_own[k];
+            if (t) {
+                atomicAdd(&cnt[i0 + k], (u64)t);
+                local_total += t;
+            }
+        }
+        __syncthreads();
+    }
+    if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+    const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = bt;
+}
+
+template <int BLOCK, int CAP, typename OffT>
+struct LargeLayout {
+    static constexpr int TS = 2 * CAP;
+    static constexpr size_t off_keys = 0;
+    static constexpr size_t off_hits = off_keys + sizeof(u32) * TS;
+    static constexpr size_t off_qd = off_hits + sizeof(u32) * TS;
+    static constexpr size_t off_qy = off_qd + sizeof(Desc<OffT>) * BLOCK;
+    static constexpr size_t bytes = off_qy + sizeof(u32) * BLOCK;
+};
+
+template <int BLOCK, int CAP, typename OffT>
+__global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
+                                                       u64 n, const Desc<OffT>* __restrict__ vdesc,
+                                                       const u32* __restrict__ headp,
+                                                       const uint2* __restrict__ ltiles, u64* __restrict__ cnt,
+                                                       u64* __restrict__ partials, Control* ctl) {
+    using L = LargeLayout<BLOCK, CAP, OffT>;
+    constexpr int NW = BLOCK / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    u32* keys = reinterpret_cast<u32*>(smem + L::off_keys);
+    u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
+    Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
+    u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
+    __shared__ u64 s_red[NW];
+    __shared__ u64 s_t;
+    __shared__ u32 s_qn;
+
+    if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u64 ntiles = *(volatile unsigned long long*)&ctl->large_tiles;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    u64 local_total = 0;
+    u32 dup = 0;
+    if (threadIdx.x == 0) s_qn = 0;
+
+    while (true) {
+        if (threadIdx.x == 0) s_t = atomicAdd(&ctl->large_next, 1ull);
+        __syncthreads();
+        const u64 t = s_t;
+        if (t >= ntiles) break;
+        const uint2 tl = ltiles[t];
+        const u64 x = tl.x;
+        const Desc<OffT> dxd = load_desc(vdesc + x);
+        const u32 dx = dxd.d;
+        const u64 fx1 = fo[x + 1];
+        const u64 a = fo[x] + (u64)tl.y * LARGE_SEG;
+        const u64 b = a + LARGE_SEG < fx1 ? a + LARGE_SEG : fx1;
+        u64 T = 0;
+        for (u32 c0 = 0; c0 < dx; c0 += CAP) {
+            const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
+            u32 lg = ceil_log2(2 * klen);
+            if (lg < 1) lg = 1;
+            const u32 size = 1u << lg;
+            for (u32 s = threadIdx.x; s < size; s += BLOCK) {
+                keys[s] = EMPTY_KEY;
+                hitc[s] = 0;
+            }
+            __syncthreads();
+            for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
+                const u32 w = __ldg(headp + (u64)dxd.start + c0 + q);
+                if (!table_insert(keys, lg, w)) dup = 1;
+            }
+            __syncthreads();
+            for (u64 e0 = a; e0 < b; e0 += BLOCK) {
+                const u64 e = e0 + threadIdx.x;
+                if (e < b) {
+                    const u32 y = __ldg(head + e);
+                    Desc<OffT> vy;
+                    vy.start = 0;
+                    vy.d = 0;
+                    if (y < n) vy = load_desc(vdesc + y);
+                    const u32 dy = vy.d;
+                    if (dy > 0 && key_less(dy, y, dx, x)) {
+                        if (dy <= (u32)LONG_LIST) {
+                            u32 hits = 0;
+                            const u64 q0 = (u64)vy.start >> 2;
+#pragma unroll
+                            for (int c = 0; c < LONG_LIST / 4; ++c) {
+                                if (4 * c < (int)dy) {
+                                    const uint4 qv = __ldg(headp4 + q0 + c);
+                                    const u32 wv[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+                                    for (int k = 0; k < 4; ++k) {
+                                        if (4 * c + k < (int)dy) {
+                                            const u32 s = table_find(keys, lg, wv[k]);
+                                            if (s != NONE) {
+                                                atomicAdd(&hitc[s], 1u);
+                                                ++hits;
+                                            }
+                                        }
+                                    }
+                                }
+                            }
+                            if (hits) {
+                                atomicAdd(&cnt[y], (u64)hits);
+                                T += hits;
+                            }
+                        } else {
+                            const u32 slot = atomicAdd(&s_qn, 1u);
+                            qd[slot] = vy;
+                            qy[slot] = y;
+                        }
+                    }
+                }
+                __syncthreads();
+                const u32 nq = s_qn;
+                for (u32 qi = warp; qi < nq; qi += NW) {
+                    const Desc<OffT> vy = qd[qi];
+                    const u32 y = qy[qi];
+                    u32 hits = 0;
+                    const u64 q0 = (u64)vy.start >> 2;
+                    for (u32 p = 4 * lane; p < vy.d; p += 128) {
+                        const uint4 qv = __ldg(headp4 + q0 + (p >> 2));
+                        const u32 wv[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            if (p + k < vy.d) {
+                                const u32 s = table_find(keys, lg, wv[k]);
+                                if (s != NONE) {
+                                    atomicAdd(&hitc[s], 1u);
+                                    ++hits;
+                                }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) hits += __shfl_down_sync(0xFFFFFFFFu, hits, o);
+                    if (lane == 0 && hits) {
+                        atomicAdd(&cnt[y], (u64)hits);
+                        T += hits;
+                    }
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) s_qn = 0;
+                __syncthreads();
+            }
+            for (u32 s = threadIdx.x; s < size; s += BLOCK) {
+                const u32 h = hitc[s];
+                if (h) atomicAdd(&cnt[keys[s]], (u64)h);
+            }
+            __syncthreads();
+        }
+        const u64 bt = block_sum_u64<BLOCK>(T, s_red);
+        if (threadIdx.x == 0 && bt) {
+            atomicAdd(&cnt[x], bt);
+            local_total += bt;
+        }
+    }
+    if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+    if (threadIdx.x == 0) partials[blockIdx.x] = local_total;
+}
+
+// Sum of the per-block partial totals (a u64 tree reduction in one block).
+__global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials, u32 np, u64* total) {
+    __shared__ u64 s_red[32];
+    u64 s = 0;
+    for (u32 i = threadIdx.x; i < np; i += 1024) s += partials[i];
+    const u64 t = block_sum_u64<1024>(s, s_red);
+    if (threadIdx.x == 0) *total = t;
+}
+
+// collect_stats: wedge_checks = sum over oriented (v,u) of |N+(u)|, the reference's counter
+// (cetric_edge_iterator.h:279-281), plus the entries streamed by the AUTO kernels.
+template <typename OffT>
+__global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
+                        const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp, Control* ctl) {
+    if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31;
+    const u64 gw = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    u64 wedge = 0, isz = 0, streamed = 0, oriented = 0;
+    for (u64 v = gw; v < n; v += nwarps) {
+        const Desc<OffT> dv = load_desc(vdesc + v);
+        if (lane == 0) oriented += dv.d;
+        for (u32 k = lane; k < dv.d; k += 32) {
+            const u32 u = headp[(u64)dv.start + k];
+            const u32 du = load_desc(vdesc + u).d;
+            wedge += du;
+            isz += (u64)dv.d + du;
+        }
+        for (u64 e = fo[v] + lane; e < fo[v + 1]; e += 32) {
+            const u32 y = head[e];
+            const u32 dy = load_desc(vdesc + y).d;
+            if (dy > 0 && key_less(dy, y, dv.d, v)) streamed += dy;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        wedge += __shfl_down_sync(0xFFFFFFFFu, wedge, o);
+        isz += __shfl_down_sync(0xFFFFFFFFu, isz, o);
+        streamed += __shfl_down_sync(0xFFFFFFFFu, streamed, o);
+        oriented += __shfl_down_sync(0xFFFFFFFFu, oriented, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&ctl->stat_wedge, wedge);
+        atomicAdd(&ctl->stat_isz, isz);
+        atomicAdd(&ctl->stat_streamed, streamed);
+        atomicAdd(&ctl->stat_oriented, oriented);
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------------
+
+namespace {
+template <typename OffT>
+using SmallL = SmallLayout<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>;
+template <typename OffT>
+using LargeL = LargeLayout<LARGE_BLOCK, LARGE_CAP, OffT>;
+
+template <typename OffT>
+int occupancy_small() {
+    static int occ = -1;
+    if (occ < 0) {
+        auto kern = k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<OffT>::bytes);
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<OffT>::bytes);
+        occ = o > 0 ? o : 1;
+    }
+    return occ;
+}
+template <typename OffT>
+int occupancy_large() {
+    static int occ = -1;
+    if (occ < 0) {
+        auto kern = k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LargeL<OffT>::bytes);
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, LARGE_BLOCK, LargeL<OffT>::bytes);
+        occ = o > 0 ? o : 1;
+    }
+    return occ;
+}
+}  // namespace
+
+template <typename OffT>
+int count_grid_small(int num_sms) {
+    return num_sms * occupancy_small<OffT>();
+}
+template <typename OffT>
+int count_grid_large(int num_sms) {
+    return num_sms * occupancy_large<OffT>();
+}
+
+template <typename OffT>
+cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
+                              const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
+                              cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large) {
+    const int gs = count_grid_small<OffT>(num_sms);
+    const int gl = count_grid_large<OffT>(num_sms);
+    const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
+    k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
+        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, cnt, partials, ctl);
+    if (after_small) cudaEventRecord(after_small, st);
+    k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
+        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs, ctl);
+    if (after_large) cudaEventRecord(after_large, st);
+    return cudaGetLastError();
+}
+
+void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st) {
+    (void)ctl;
+    k_final<<<1, 1024, 0, st>>>(partials, np, total);
+}
+
+template <typename OffT>
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
+                  int num_sms, cudaStream_t st) {
+    if (n == 0) return;
+    k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp, ctl);
+}
+
+template int count_grid_small<u32>(int);
+template int count_grid_small<u64>(int);
+template int count_grid_large<u32>(int);
+template int count_grid_large<u64>(int);
+template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
+template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
+template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
+template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
+
+}  // namespace ktri

@@ -1,0 +1,54 @@
+// Internal declarations shared by the host code and the CUDA launchers.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ktri.h"
+
+struct ktri_graph {
+    uint64_t n = 0;
+    std::vector<uint64_t> first_out;
+    std::vector<uint32_t> head;
+};
+
+namespace ktri {
+
+// Resolved options (defaults filled in).
+struct Options {
+    int32_t method = KTRI_METHOD_AUTO;
+    uint32_t small_outdegree = 32;
+    bool collect_stats = false;
+    uint64_t binary_cutoff = 1000;
+    double hybrid_scale = 1.0;
+};
+
+// Device-side error bits written by the kernels (one u32 word in the control block).
+enum : uint32_t {
+    DEV_ERR_ID_RANGE = 1u << 0,   // head entry >= n
+    DEV_ERR_SELF_LOOP = 1u << 1,  // head entry == owner
+    DEV_ERR_DUPLICATE = 1u << 2,  // a list holds the same id twice
+    DEV_ERR_DEGREE = 1u << 3,     // first_out not monotone, or a degree >= 2^32
+    DEV_FLAG_UNSORTED = 1u << 8,  // some input list is not strictly increasing (not an error)
+};
+
+// Control block in device memory: counters and flags the kernels share.
+struct Control {
+    uint32_t err;              // DEV_ERR_* | DEV_FLAG_*
+    uint32_t pad0;
+    unsigned long long large_tiles;      // number of (owner, segment) tiles for large owners
+    unsigned long long small_next;       // dynamic tile cursor of the small-owner kernel
+    unsigned long long large_next;       // dynamic tile cursor of the large-owner kernel
+    unsigned long long spanning;         // number of vertices whose out-list was assembled by several tiles
+    unsigned long long edge_next;        // dynamic cursor of the per-edge kernels
+    unsigned long long stat_wedge;       // collect_stats: sum of |N+(u)| over oriented (v,u)
+    unsigned long long stat_isz;         // collect_stats: sum of |N+(v)|+|N+(u)|
+    unsigned long long stat_streamed;    // collect_stats: entries streamed by the AUTO kernels
+    unsigned long long stat_oriented;    // collect_stats: sum of out-degrees
+    unsigned long long sort_mid;         // lists sorted by whole blocks in shared memory
+    unsigned long long sort_big;         // lists sorted by whole blocks in global scratch
+    unsigned long long pad[4];
+};
+
+}  // namespace ktri

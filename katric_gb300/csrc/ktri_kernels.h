@@ -1,0 +1,79 @@
+// Launchers of the device kernels (host-callable, no torch types).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ktri_internal.h"
+
+namespace ktri {
+
+using u32 = uint32_t;
+using u64 = unsigned long long;
+
+constexpr int ORIENT_BLOCK = 256;
+constexpr int ORIENT_IPT = 8;
+constexpr int SMALL_BLOCK = 256;
+constexpr int SMALL_IPT = 4;
+constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
+constexpr int LARGE_BLOCK = 256;
+constexpr int LARGE_CAP = 4096;      // keys per shared-memory table chunk of the vertex kernel
+constexpr u32 LARGE_SEG = 2048;      // adjacency slots per (owner, segment) tile
+constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
+
+inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
+inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d) {
+    u64 owners = nnz / ((u64)small_d + 1) + 1;
+    if (owners > n) owners = n;
+    return owners + nnz / LARGE_SEG + 1;
+}
+
+void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, Control* ctl, int num_sms,
+                 cudaStream_t st);
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, u32* headp, u32* dplus,
+                   u32* spanning, Control* ctl, cudaStream_t st);
+template <typename OffT>
+void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
+                 Control* ctl, int num_sms, cudaStream_t st);
+
+// Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
+template <typename OffT>
+int count_grid_small(int num_sms);
+template <typename OffT>
+int count_grid_large(int num_sms);
+template <typename OffT>
+cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
+                              const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
+                              cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
+void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
+
+// Work counters of the reference (wedge_checks, intersection_size_local) and of the AUTO
+// kernels, accumulated into the control block.
+template <typename OffT>
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
+                  int num_sms, cudaStream_t st);
+
+// Sorted-list strategies (merge, binary search, binary, hybrid): sort out-lists by id, then
+// one warp per oriented edge.
+template <typename OffT>
+void launch_sort_lists(u64 n, const void* vdesc, u32* headp, u32* mid_list, u32* big_list, u32* scratch,
+                       u64 scratch_per_block, int big_grid, Control* ctl, int num_sms, cudaStream_t st);
+template <typename OffT>
+void launch_count_edges(u64 n, const void* vdesc, const u32* headp, int method, u64 cutoff, double hybrid_scale,
+                        u64* cnt, u64* partials, int grid, Control* ctl, cudaStream_t st);
+int count_grid_edges(int num_sms);
+
+// Oriented CSR export: compact copy of the out-lists (after sorting).
+template <typename OffT>
+void launch_export(u64 n, const void* vdesc, const u32* headp, const u64* out_fo, u32* out_head, int num_sms,
+                   cudaStream_t st);
+template <typename OffT>
+void launch_outdeg(u64 n, const void* vdesc, u64* out, int num_sms, cudaStream_t st);
+
+// Batched pair intersection for known-answer tests of the strategies.
+void launch_intersect_pairs(int method, const u32* a_vals, const u64* a_off, const u32* b_vals, const u64* b_off,
+                            u64 npairs, u64 cutoff, double hybrid_scale, u64* counts, u32* members, int* err,
+                            cudaStream_t st);
+
+}  // namespace ktri

@@ -1,0 +1,258 @@
+// Orientation: degrees, (degree, id) orientation with order-preserving compaction of every
+// adjacency list to its out-neighbours, and the per-vertex out-list descriptors.
+//
+// Restates on the device what DistributedGraph::orient (distributed_graph.h:538-566) with
+// node_ordering::degree_outward (distributed_graph.h:148-163) computes: u is kept in the
+// out-list of v iff (deg(v), v) < (deg(u), u).  The reference partitions each list in place;
+// here the input CSR is read-only and the out-lists are written to a separate gapped array.
+// A list that one merge-path tile holds entirely keeps its input order.  A list that spans
+// tiles is assembled from per-tile pieces and is recorded in the spanning list; the id sort
+// (sort_neighborhoods, distributed_graph.h:578-593) runs only where a strategy needs sorted
+// lists.
+#include "ktri_device.cuh"
+#include "ktri_kernels.h"
+
+namespace ktri {
+
+// deg[v] = first_out[v+1] - first_out[v]; zero the out-degrees and the per-vertex counts.
+__global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restrict__ deg, u32* __restrict__ dplus,
+                       u64* __restrict__ cnt, Control* ctl) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    u32 err = 0;
+    for (u64 v = (u64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        u64 a = fo[v], b = fo[v + 1];
+        u32 d = 0;
+        if (b < a || b - a > 0xFFFFFFFFull || b > nnz) err |= DEV_ERR_DEGREE;
+        else d = (u32)(b - a);
+        deg[v] = d;
+        dplus[v] = 0;
+        if (cnt) cnt[v] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (fo[0] != 0 || fo[n] != nnz)) err |= DEV_ERR_DEGREE;
+    if (err) atomicOr(&ctl->err, err);
+}
+
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
+                                                  u64 nnz, const u32* __restrict__ deg, u32* __restrict__ headp,
+                                                  u32* __restrict__ dplus, u32* __restrict__ spanning,
+                                                  Control* ctl) {
+    constexpr int TILE = BLOCK * IPT;
+    __shared__ u64 s_fo[TILE + 2];
+    __shared__ u32 s_head[TILE];
+    __shared__ u32 s_cnt[TILE + 2];
+    __shared__ u32 s_first[TILE + 2];
+    __shared__ u32 s_warp[BLOCK / 32];
+    __shared__ u64 s_b[2];
+    __shared__ u32 s_carry[2];
+
+    if (ctl->err & DEV_ERR_MASK) return;
+    const u64 total = n + nnz;
+    const u64 d0 = (u64)blockIdx.x * TILE;
+    if (d0 >= total) return;
+    const u64 d1 = d0 + TILE < total ? d0 + TILE : total;
+    if (threadIdx.x == 0) s_b[0] = mp_search(fo, n, d0);
+    if (threadIdx.x == 32) s_b[1] = mp_search(fo, n, d1);
+    __syncthreads();
+    const u64 i0 = s_b[0], i1 = s_b[1];
+    const u64 j0 = d0 - i0, j1 = d1 - i1;
+    const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
+    const u32 nfo = (u32)(fo_last - i0 + 1);
+    for (u32 k = threadIdx.x; k < nfo; k += BLOCK) {
+        s_fo[k] = fo[i0 + k];
+        s_cnt[k] = 0;
+    }
+    const u32 nslot = (u32)(j1 - j0);
+    for (u32 k = threadIdx.x; k < nslot; k += BLOCK) s_head[k] = head[j0 + k];
+    __syncthreads();
+
+    // this thread's run of the merge path
+    const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
+    const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
+    const u64 i_start = mp_search_window(s_fo, i0, i0, i1, dt);
+    const u64 j_start = dt - i_start;
+
+    u32 own[IPT], yv[IPT];
+    bool unsorted = false;
+    u32 err = 0;
+    {
+        u64 i = i_start, j = j_start;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            own[k] = NONE;
+            yv[k] = 0;
+            if (dt + k < dte) {
+                if (i < n && j < s_fo[i + 1 - i0]) {
+                    own[k] = (u32)(i - i0);
+                    u32 y = s_head[j - j0];
+                    yv[k] = y;
+                    if (j + 1 < s_fo[i + 1 - i0]) {
+                        u32 nx = (j + 1 < j1) ? s_head[j + 1 - j0] : __ldg(head + j + 1);
+                        if (nx < y) unsorted = true;
+                        if (nx == y) err |= DEV_ERR_DUPLICATE;
+                    }
+                    ++j;
+                } else {
+                    ++i;
+                }
+            }
+        }
+    }
+    u32 dy[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) dy[k] = (own[k] != NONE && yv[k] < n) ? __ldg(deg + yv[k]) : 0u;
+
+    u32 outbits = 0;
+    {
+        u32 run_owner = NONE, run = 0;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            if (own[k] == NONE) continue;
+            const u64 x = i0 + own[k];
+            const u32 y = yv[k];
+            bool out = false;
+            if (y >= n) err |= DEV_ERR_ID_RANGE;
+            else if ((u64)y == x) err |= DEV_ERR_SELF_LOOP;
+            else out = key_less(s_fo[own[k] + 1] - s_fo[own[k]], x, dy[k], y);
+            if (own[k] != run_owner) {
+                if (run) atomicAdd(&s_cnt[run_owner], run);
+                run_owner = own[k];
+                run = 0;
+            }
+            if (out) {
+                outbits |= 1u << k;
+                ++run;
+            }
+        }
+        if (run) atomicAdd(&s_cnt[run_owner], run);
+    }
+    if (err) atomicOr(&ctl->err, err);
+    if (unsorted) atomicOr(&ctl->err, DEV_FLAG_UNSORTED);
+
+    u32 tot;
+    const u32 base = block_exclusive_scan<BLOCK>((u32)__popc(outbits), s_warp, &tot);
+
+    // first in-tile slot of every owner: record its scan position; lists wholly inside the
+    // tile publish their out-degree here
+    {
+        u32 run = base;
+        u64 j = j_start;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            if (own[k] == NONE) continue;
+            const u32 o = own[k];
+            const u64 first = s_fo[o] > j0 ? s_fo[o] : j0;
+            if (j == first) {
+                s_first[o] = run;
+                if (s_fo[o] >= j0 && s_fo[o + 1] <= j1) dplus[i0 + o] = s_cnt[o];
+            }
+            if (outbits >> k & 1u) ++run;
+            ++j;
+        }
+    }
+    if (threadIdx.x == 0) {
+        s_carry[0] = 0;
+        s_carry[1] = 0;
+        if (i0 < n) {
+            const u64 a = s_fo[0], b = s_fo[1];
+            const u64 lo = a > j0 ? a : j0, hi = b < j1 ? b : j1;
+            if (lo < hi && (a < j0 || b > j1)) {
+                s_carry[0] = atomicAdd(&dplus[i0], s_cnt[0]);
+                if (a >= j0) spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)i0;
+            }
+        }
+        if (i1 != i0 && i1 < n) {
+            const u64 a = s_fo[i1 - i0], b = s_fo[i1 - i0 + 1];
+            if (a < j1 && b > j1) {
+                s_carry[1] = atomicAdd(&dplus[i1], s_cnt[i1 - i0]);
+                spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)i1;
+            }
+        }
+    }
+    __syncthreads();
+    {
+        u32 run = base;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            if (!(outbits >> k & 1u)) continue;
+            const u32 o = own[k];
+            const u64 x = i0 + o;
+            const u32 carry = (x == i0) ? s_carry[0] : (x == i1 ? s_carry[1] : 0u);
+            const u64 pos = (u64)(run - s_first[o]) + carry;
+            headp[oriented_start(s_fo[o], x) + pos] = yv[k];
+            ++run;
+        }
+    }
+}
+
+// Out-list descriptors, and the (owner, segment) tiles of owners above the small
+// out-degree threshold.
+template <typename OffT>
+__global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict__ dplus, Desc<OffT>* __restrict__ vdesc,
+                       uint2* __restrict__ ltiles, u32 small_d, u32 seg, Control* ctl) {
+    if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31;
+    const u64 warp_global = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 base = warp_global * 32; base < n; base += nwarps * 32) {
+        const u64 v = base + lane;
+        u32 nt = 0;
+        if (v < n) {
+            const u64 a = fo[v], b = fo[v + 1];
+            const u32 d = dplus[v];
+            Desc<OffT> ds;
+            ds.start = (OffT)oriented_start(a, v);
+            ds.d = d;
+            if constexpr (sizeof(OffT) == 8) ds.pad = 0;
+            vdesc[v] = ds;
+            if (d > small_d) nt = (u32)((b - a + seg - 1) / seg);
+        }
+        // warp-aggregated reservation of tile slots
+        u32 incl = nt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const u32 wsum = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        u64 wbase = 0;
+        if (lane == 31 && wsum) wbase = atomicAdd(&ctl->large_tiles, (u64)wsum);
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+        const u64 my = wbase + incl - nt;
+        for (u32 s = 0; s < nt; ++s) ltiles[my + s] = make_uint2((u32)v, s);
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------------
+
+void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, Control* ctl, int num_sms,
+                 cudaStream_t st) {
+    if (n == 0) return;
+    u64 blocks = (n + 255) / 256;
+    u64 cap = (u64)num_sms * 8;
+    k_prep<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(fo, n, nnz, deg, dplus, cnt, ctl);
+}
+
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, u32* headp, u32* dplus,
+                   u32* spanning, Control* ctl, cudaStream_t st) {
+    constexpr int BLOCK = ORIENT_BLOCK, IPT = ORIENT_IPT;
+    const u64 total = n + nnz;
+    if (total == 0) return;
+    const u64 tiles = (total + BLOCK * IPT - 1) / (BLOCK * IPT);
+    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, headp, dplus, spanning, ctl);
+}
+
+template <typename OffT>
+void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
+                 Control* ctl, int num_sms, cudaStream_t st) {
+    if (n == 0) return;
+    u64 blocks = (n + 255) / 256;
+    u64 cap = (u64)num_sms * 8;
+    k_desc<OffT><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(
+        fo, n, dplus, reinterpret_cast<Desc<OffT>*>(vdesc), ltiles, small_d, seg, ctl);
+}
+
+template void launch_desc<u32>(const u64*, u64, const u32*, void*, uint2*, u32, u32, Control*, int, cudaStream_t);
+template void launch_desc<u64>(const u64*, u64, const u32*, void*, uint2*, u32, u32, Control*, int, cudaStream_t);
+
+}  // namespace ktri

@@ -1,0 +1,136 @@
+"""Host graphs: CSR containers, seeded generators and the reference's file formats.
+
+A Graph holds an undirected simple graph as CSR (u64 first_out[n+1], u32 head[nnz]), the
+layout the counting entry points take.  Generators and readers run in libktri.so's host
+code (C++ with OpenMP), so the same seed gives the same graph on every host.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+
+class Graph:
+    """CSR graph on the host.  first_out: u64[n+1], head: u32[nnz]."""
+
+    def __init__(self, first_out, head, *, _handle=None):
+        self.first_out = np.ascontiguousarray(first_out, dtype=np.uint64)
+        self.head = np.ascontiguousarray(head, dtype=np.uint32)
+        self._handle = _handle  # keeps native memory alive when the arrays are views of it
+        if len(self.first_out) == 0:
+            raise ValueError("first_out needs n+1 entries")
+
+    @property
+    def n(self) -> int:
+        return len(self.first_out) - 1
+
+    @property
+    def nnz(self) -> int:
+        return len(self.head)
+
+    @property
+    def m(self) -> int:
+        """Undirected edges (each stored twice)."""
+        return self.nnz // 2
+
+    def degree(self) -> np.ndarray:
+        return np.diff(self.first_out)
+
+    def wedges(self) -> int:
+        """sum over v of deg(v) choose 2 (apps/shmetric.cpp:120-129)."""
+        d = self.degree().astype(np.uint64)
+        return int(np.sum(d * (d - 1) // 2, dtype=np.uint64)) if len(d) else 0
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None:
+            try:
+                _native.load(build_if_missing=False).ktri_graph_free(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    # ---- construction -------------------------------------------------------------------
+    @staticmethod
+    def _from_handle(h) -> "Graph":
+        L = _native.load()
+        n = L.ktri_graph_n(h)
+        nnz = L.ktri_graph_nnz(h)
+        fo_ptr = L.ktri_graph_first_out(h)
+        hd_ptr = L.ktri_graph_head(h)
+        fo = np.ctypeslib.as_array((ctypes.c_uint64 * (n + 1)).from_address(fo_ptr)) if n + 1 else np.zeros(1, np.uint64)
+        hd = np.ctypeslib.as_array((ctypes.c_uint32 * nnz).from_address(hd_ptr)) if nnz else np.zeros(0, np.uint32)
+        return Graph(fo, hd, _handle=h)
+
+    @staticmethod
+    def _call(fn, *args) -> "Graph":
+        h = ctypes.c_void_p()
+        _native.check(fn(*args, ctypes.byref(h)))
+        return Graph._from_handle(h)
+
+    @classmethod
+    def gnm(cls, n: int, m: int, seed: int = 1) -> "Graph":
+        """G(n,m): m distinct undirected edges uniformly at random, no self-loops."""
+        return cls._call(_native.load().ktri_graph_gnm, n, m, seed)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 2) -> "Graph":
+        """RMAT with 2^scale vertices and edge_factor*2^scale samples; symmetrised, deduplicated, no loops."""
+        return cls._call(_native.load().ktri_graph_rmat, scale, edge_factor, a, b, c, seed)
+
+    @classmethod
+    def rgg2d(cls, n: int, avg_degree: float = 32.0, seed: int = 3) -> "Graph":
+        """2D random geometric graph in the unit square, ids in Morton order of the points."""
+        return cls._call(_native.load().ktri_graph_rgg2d, n, avg_degree, seed)
+
+    @classmethod
+    def read_metis(cls, path: str) -> "Graph":
+        return cls._call(_native.load().ktri_graph_read_metis, path.encode())
+
+    @classmethod
+    def read_binary(cls, stem: str) -> "Graph":
+        """<stem>.first_out (u64[n+1]) + <stem>.head (u64[nnz]), the reference's binary input format."""
+        return cls._call(_native.load().ktri_graph_read_binary, stem.encode())
+
+    @classmethod
+    def read(cls, path: str, input_format: str = "metis") -> "Graph":
+        """graphio::read_graph(file, format) equivalent (apps/shmetric.cpp:119)."""
+        fmt = input_format.lower()
+        if fmt == "metis":
+            return cls.read_metis(path)
+        if fmt == "binary":
+            return cls.read_binary(path)
+        raise ValueError(f"unknown input format {input_format!r} (metis or binary)")
+
+    def _native_handle(self):
+        if self._handle is not None:
+            return self._handle
+        h = ctypes.c_void_p()
+        L = _native.load()
+        _native.check(L.ktri_graph_from_csr(self.n, self.first_out.ctypes.data,
+                                            self.head.ctypes.data if self.nnz else None, ctypes.byref(h)))
+        self._handle = h
+        return h
+
+    def write_binary(self, stem: str) -> None:
+        _native.check(_native.load().ktri_graph_write_binary(self._native_handle(), stem.encode()))
+
+    def write_metis(self, path: str) -> None:
+        _native.check(_native.load().ktri_graph_write_metis(self._native_handle(), path.encode()))
+
+
+def generate(name: str, seed: int | None = None, **kw) -> Graph:
+    """Named generator (the subset of --gen the engine is measured on): gnm, rmat, rgg2d."""
+    name = name.lower()
+    if name in ("gnm", "gnm_undirected"):
+        return Graph.gnm(kw["n"], kw["m"], 1 if seed is None else seed)
+    if name == "rmat":
+        return Graph.rmat(kw["scale"], kw.get("edge_factor", 16), kw.get("a", 0.57), kw.get("b", 0.19),
+                          kw.get("c", 0.19), 2 if seed is None else seed)
+    if name in ("rgg2d", "rgg_2d"):
+        return Graph.rgg2d(kw["n"], kw.get("avg_degree", 32.0), 3 if seed is None else seed)
+    raise ValueError(f"unknown generator {name!r}")

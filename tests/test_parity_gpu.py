@@ -1,0 +1,200 @@
+"""Parity of the CUDA path with the CPU oracle, through the C ABI (needs a GB300).
+
+Bar: bit-exact u64 totals and per-vertex counts for every intersection method, on the
+reference's example graphs, on the small G(n,m) workload (n=2^14, m=2^17, seed 1) and on
+seeded RMAT / RGG graphs at sizes the oracle finishes in seconds; unsorted input lists;
+edge cases (empty, edgeless, single triangle, star, cliques whose out-lists need chunked
+tables); invalid CSR reported as KTRI_ERR_INVALID_CSR.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from katric_gb300 import Config, Graph, KtriError, _native
+
+pytestmark = pytest.mark.gpu
+
+GPU_METHODS = ["auto", "merge", "binary-search", "binary", "hybrid"]
+
+
+def check_parity(counter, oracle, fo, hd, methods=GPU_METHODS, threads=8):
+    total, pv, _ = oracle.count(fo, hd, method="merge", num_threads=threads)
+    for m in methods:
+        t, p = counter.count(fo, hd, Config(intersection_method=m))
+        assert t == total, (m, t, total)
+        assert np.array_equal(p, pv), m
+    return total
+
+
+def csr_from_edges(n, edges, shuffle_seed=None):
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+    src = np.concatenate([e[:, 0], e[:, 1]])
+    dst = np.concatenate([e[:, 1], e[:, 0]])
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    fo = np.zeros(n + 1, dtype=np.uint64)
+    fo[1:] = np.cumsum(np.bincount(src, minlength=n))
+    hd = dst.astype(np.uint32)
+    if shuffle_seed is not None:
+        rng = np.random.default_rng(shuffle_seed)
+        for v in range(n):
+            rng.shuffle(hd[int(fo[v]):int(fo[v + 1])])
+    return fo, hd
+
+
+def test_examples(counter, oracle, golden):
+    ex, _ = golden
+    for g in ex["graphs"]:
+        t = check_parity(counter, oracle, g["first_out"], g["head"])
+        assert t == g["triangles"], g["name"]
+
+
+def test_gnm_small_workload(counter, oracle):
+    g = Graph.gnm(1 << 14, 1 << 17, seed=1)
+    check_parity(counter, oracle, g.first_out, g.head)
+
+
+@pytest.mark.parametrize("scale", [10, 14, 16])
+def test_rmat(counter, oracle, scale):
+    g = Graph.rmat(scale, 16, seed=2)
+    check_parity(counter, oracle, g.first_out, g.head)
+
+
+@pytest.mark.parametrize("n", [1 << 12, 1 << 16])
+def test_rgg(counter, oracle, n):
+    g = Graph.rgg2d(n, 32.0, seed=3)
+    check_parity(counter, oracle, g.first_out, g.head)
+
+
+def test_unsorted_lists(counter, oracle):
+    g = Graph.rmat(13, 16, seed=5)
+    fo = g.first_out
+    hd = g.head.copy()
+    rng = np.random.default_rng(1)
+    for v in range(g.n):
+        a, b = int(fo[v]), int(fo[v + 1])
+        rng.shuffle(hd[a:b])
+    check_parity(counter, oracle, fo, hd)
+    assert counter.stats().input_sorted == 0
+
+
+def test_empty_and_edgeless(counter):
+    t, p = counter.count(np.zeros(1, np.uint64), np.zeros(0, np.uint32))
+    assert t == 0 and len(p) == 0
+    t, p = counter.count(np.zeros(6, np.uint64), np.zeros(0, np.uint32))
+    assert t == 0 and (p == 0).all() and len(p) == 5
+
+
+def test_single_triangle_and_star(counter, oracle):
+    fo, hd = csr_from_edges(4, [(0, 1), (1, 2), (0, 2)])
+    assert check_parity(counter, oracle, fo, hd) == 1
+    star = [(0, i) for i in range(1, 3000)] + [(1, 2), (5, 6)]
+    fo, hd = csr_from_edges(3000, star)
+    assert check_parity(counter, oracle, fo, hd) == 2
+
+
+@pytest.mark.parametrize("k", [40, 700])
+def test_cliques(counter, oracle, k):
+    """Cliques: every vertex has the same degree, so ties in (degree, id) decide the orientation."""
+    edges = [(a, b) for a in range(k) for b in range(a + 1, k)]
+    fo, hd = csr_from_edges(k + 3, edges + [(k, k + 1)], shuffle_seed=3)
+    t = check_parity(counter, oracle, fo, hd)
+    assert t == k * (k - 1) * (k - 2) // 6
+
+
+def test_big_clique_chunked_tables(counter):
+    """K_4200: out-degrees up to 4199 exceed one shared-memory table chunk (4096 keys).
+    Checked against the closed form (the oracle would take minutes)."""
+    k = 4200
+    a, b = np.triu_indices(k, 1)
+    fo, hd = csr_from_edges(k + 3, list(zip(a.tolist(), b.tolist())) + [(k, k + 1)])
+    t, pv = counter.count(fo, hd, Config(intersection_method="auto"))
+    assert t == k * (k - 1) * (k - 2) // 6
+    assert (pv[:k] == (k - 1) * (k - 2) // 2).all() and (pv[k:] == 0).all()
+
+
+def test_many_components_mixed(counter, oracle):
+    """Disjoint union of a hub-heavy RMAT, an RGG and cliques: tiles mix small and large owners."""
+    parts = [Graph.rmat(11, 16, seed=9), Graph.rgg2d(3000, 24.0, seed=4), Graph.gnm(500, 20000, seed=8)]
+    fo = [0]
+    hd = []
+    off = 0
+    for g in parts:
+        f = g.first_out.astype(np.int64)
+        for v in range(g.n):
+            hd.extend((g.head[f[v]:f[v + 1]].astype(np.int64) + off).tolist())
+            fo.append(len(hd))
+        off += g.n
+    check_parity(counter, oracle, np.array(fo, np.uint64), np.array(hd, np.uint32))
+
+
+def test_invalid_csr(counter):
+    fo = np.array([0, 2, 3, 4], dtype=np.uint64)
+    with pytest.raises(KtriError) as e:  # self-loop 0-0
+        counter.count(fo, np.array([0, 1, 0, 0], dtype=np.uint32))
+    assert e.value.code == _native.ERR_INVALID_CSR
+    with pytest.raises(KtriError) as e:  # id out of range
+        counter.count(fo, np.array([1, 7, 0, 0], dtype=np.uint32))
+    assert e.value.code == _native.ERR_INVALID_CSR
+    with pytest.raises(KtriError) as e:  # non-monotone offsets
+        counter.count(np.array([0, 3, 1, 4], dtype=np.uint64), np.array([1, 2, 0, 0], dtype=np.uint32))
+    assert e.value.code == _native.ERR_INVALID_CSR
+    with pytest.raises(KtriError) as e:  # duplicate entry in a sorted list
+        counter.count(np.array([0, 2, 3, 4], dtype=np.uint64), np.array([1, 1, 0, 0], dtype=np.uint32))
+    assert e.value.code == _native.ERR_INVALID_CSR
+    # the context stays usable after errors
+    f2, h2 = csr_from_edges(3, [(0, 1), (1, 2), (0, 2)])
+    assert counter.count(f2, h2)[0] == 1
+
+
+def test_stats_match_reference_counters(counter, oracle):
+    g = Graph.rmat(12, 16, seed=2)
+    total, _, st = oracle.count(g.first_out, g.head, num_threads=4)
+    t, _ = counter.count(g.first_out, g.head, Config(collect_stats=True))
+    rs = counter.stats()
+    assert t == total
+    assert rs.wedge_checks == st["wedge_checks"]
+    assert rs.intersection_size_local == st["intersection_size_local"]
+    assert rs.oriented_edges * 2 == g.nnz
+    assert rs.streamed_entries <= rs.wedge_checks
+
+
+def test_orientation_export(counter, oracle, golden):
+    ex, _ = golden
+    graphs = [(g["first_out"], g["head"]) for g in ex["graphs"]]
+    big = Graph.rmat(12, 16, seed=6)
+    graphs.append((big.first_out, big.head))
+    for fo, hd in graphs:
+        ofo, oh = counter.orient(fo, hd)
+        efo, eh = oracle.oriented_csr(fo, hd)
+        assert np.array_equal(ofo, efo)
+        assert np.array_equal(oh, eh)
+
+
+@pytest.mark.parametrize("method", GPU_METHODS)
+def test_intersection_kat_gpu(counter, golden, method):
+    _, kat = golden
+    pairs = []
+    expect = []
+    for a, b, e in kat["triples"]:
+        pairs += [(a, b), (b, a)]
+        expect += [e, e]
+    got = counter.intersect_pairs(pairs, method=method)
+    for g, e in zip(got, expect):
+        assert (sorted(g) if method in ("binary", "auto") else g) == e
+
+
+@pytest.mark.parametrize("method", GPU_METHODS)
+def test_intersection_random_gpu(counter, method):
+    rng = np.random.default_rng(11)
+    pairs = []
+    for _ in range(200):
+        na, nb = rng.integers(0, 1500, size=2)
+        hi = int(rng.choice([100, 5000, 1 << 30]))
+        a = np.unique(rng.integers(1, hi, size=na)).astype(np.uint32)
+        b = np.unique(rng.integers(1, hi, size=nb)).astype(np.uint32)
+        pairs.append((a, b))
+    got = counter.intersect_pairs(pairs, method=method)
+    for (a, b), g in zip(pairs, got):
+        assert sorted(g) == np.intersect1d(a, b).tolist()
