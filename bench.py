@@ -32,6 +32,10 @@ WORKLOADS = {
     "rmat24": dict(kind="rmat", scale=24, edge_factor=16, seed=2),
     "rgg24": dict(kind="rgg2d", n=1 << 24, avg_degree=32.0, seed=3),
     "gnm14": dict(kind="gnm", n=1 << 14, m=1 << 17, seed=1),
+    # smaller cases of the same generators (profiling captures, quick checks)
+    "rmat20": dict(kind="rmat", scale=20, edge_factor=16, seed=2),
+    "rmat22": dict(kind="rmat", scale=22, edge_factor=16, seed=2),
+    "rgg20": dict(kind="rgg2d", n=1 << 20, avg_degree=32.0, seed=3),
 }
 METRIC = "edges/s (undirected edges / time of one exact total + per-vertex count)"
 KERNELS_PER_STEP = 6  # k_prep, k_orient, k_desc, k_count_small, k_count_large, k_final
