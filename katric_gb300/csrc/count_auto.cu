@@ -15,13 +15,34 @@
 // Two kernels split the owners by out-degree:
 //   k_count_small: owners with out-degree <= SMALL_D.  Merge-path tiles over the adjacency
 //     (as in orientation) give every block the same number of slots; the tables of all
-//     owners in a tile live side by side in shared memory.
+//     owners in a tile live side by side in shared memory.  Selected edges are queued,
+//     counting-sorted by streamed-list length so that the lanes of a warp carry equal work,
+//     then streamed one list per thread with uint4 loads.
 //   k_count_large: owners above SMALL_D, one (owner, segment of LARGE_SEG slots) tile per
-//     block iteration; long streamed lists are shared out to whole warps.
+//     block iteration.  Short streamed lists are handled one per thread while the segment is
+//     scanned; longer ones are queued and taken one at a time by whole warps (one entry per
+//     lane, two loads in flight), so no block-wide barrier separates the lists.
 #include "ktri_device.cuh"
 #include "ktri_kernels.h"
 
 namespace ktri {
+
+// Probe key w in the open-addressing table keys[0, mask] (linear probing, multiplicative
+// hash, 32-lg = shift).  On a hit, count it in the slot's counter.  Tables are at most half
+// full, so an empty slot ends every miss.
+__device__ __forceinline__ u32 probe_hit(const u32* keys, u32* hits, u32 shift, u32 mask, u32 w) {
+    u32 s = (w * 0x9E3779B1u) >> shift;
+    for (u32 it = 0; it <= mask; ++it) {
+        const u32 k = keys[s];
+        if (k == w) {
+            atomicAdd(&hits[s], 1u);
+            return 1u;
+        }
+        if (k == EMPTY_KEY) return 0u;
+        s = (s + 1) & mask;
+    }
+    return 0u;
+}
 
 template <int BLOCK, int IPT, int SD, typename OffT>
 struct SmallLayout {
@@ -36,17 +57,24 @@ struct SmallLayout {
     static constexpr size_t off_own = off_ko + sizeof(u32) * (TILE + 2);
     static constexpr size_t off_keys = off_own + sizeof(u32) * (TILE + 2);
     static constexpr size_t off_hits = off_keys + sizeof(u32) * TBL;
-    static constexpr size_t bytes = off_hits + sizeof(u32) * TBL;
+    static constexpr size_t off_qy = off_hits + sizeof(u32) * TBL;
+    static constexpr size_t off_qs = off_qy + sizeof(u32) * TILE;
+    static constexpr size_t off_qm = off_qs + sizeof(OffT) * TILE;
+    static constexpr size_t off_ord = off_qm + sizeof(u32) * TILE;
+    static constexpr size_t bytes = off_ord + sizeof(unsigned short) * TILE;
 };
 
 template <int BLOCK, int IPT, int SD, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
-                                                       const u32* __restrict__ headp, u64* __restrict__ cnt,
+                                                       const u32* __restrict__ headp,
+                                                       const u32* __restrict__ tile_i0, u64* __restrict__ cnt,
                                                        u64* __restrict__ partials, Control* ctl) {
     using L = SmallLayout<BLOCK, IPT, SD, OffT>;
+    static_assert(L::TILE == TILE_BASE, "one counting tile = one base tile");
     constexpr int TILE = L::TILE;
     constexpr int WPT = L::WPT;
+    static_assert(SD < 64, "list length is packed in 6 bits");
     extern __shared__ __align__(16) unsigned char smem[];
     u64* s_fo = reinterpret_cast<u64*>(smem + L::off_fo);
     Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
@@ -56,11 +84,18 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
     u32* s_own = reinterpret_cast<u32*>(smem + L::off_own);
     u32* s_keys = reinterpret_cast<u32*>(smem + L::off_keys);
     u32* s_hits = reinterpret_cast<u32*>(smem + L::off_hits);
+    u32* q_y = reinterpret_cast<u32*>(smem + L::off_qy);
+    OffT* q_s = reinterpret_cast<OffT*>(smem + L::off_qs);
+    u32* q_m = reinterpret_cast<u32*>(smem + L::off_qm);
+    unsigned short* q_ord = reinterpret_cast<unsigned short*>(smem + L::off_ord);
     __shared__ u32 s_warp[BLOCK / 32];
     __shared__ u64 s_red[BLOCK / 32];
     __shared__ u64 s_b[3];
+    __shared__ u32 s_bins[SD + 2];
+    __shared__ u32 s_qn;
 
     if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31;
     const u64 total_items = n + nnz;
     const u64 ntiles = (total_items + TILE - 1) / TILE;
     const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
@@ -69,13 +104,17 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
 
     while (true) {
         if (threadIdx.x == 0) s_b[2] = atomicAdd(&ctl->small_next, 1ull);
+        if (threadIdx.x < SD + 2) s_bins[threadIdx.x] = 0;
+        if (threadIdx.x == 0) s_qn = 0;
         __syncthreads();
         const u64 tile = s_b[2];
         if (tile >= ntiles) break;
         const u64 d0 = tile * TILE;
         const u64 d1 = d0 + TILE < total_items ? d0 + TILE : total_items;
-        if (threadIdx.x == 0) s_b[0] = mp_search(fo, n, d0);
-        if (threadIdx.x == 32) s_b[1] = mp_search(fo, n, d1);
+        if (threadIdx.x == 0) {
+            s_b[0] = tile_i0[tile];
+            s_b[1] = tile_i0[tile + 1];
+        }
         __syncthreads();
         const u64 i0 = s_b[0], i1 = s_b[1];
         if (i0 >= n) {  // only trailing vertex-end events: nothing to count
@@ -149,12 +188,11 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             const u32 w = __ldg(headp + (u64)s_desc[lo].start + (q - s_ko[lo]));
             if (!table_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
         }
-        __syncthreads();
 
-        // walk this thread's items of the merge path
+        // walk this thread's items of the merge path and queue the edges this tile owns
         const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
         const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
-        const u64 i_start = mp_search_window(s_fo, i0, i0, i1 < fo_last ? i1 : fo_last, dt);
+        const u64 i_start = mp_search_window(s_fo, i0, i0, i1, dt);
         u32 own[IPT], yv[IPT];
         {
             u64 i = i_start, j = dt - i_start;
@@ -165,7 +203,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
                 if (dt + k < dte) {
                     if (i < n && j < s_fo[i + 1 - i0]) {
                         const u32 o = (u32)(i - i0);
-                        if (s_tb[o] != NONE) {
+                        const u32 d = s_desc[o].d;
+                        if (d > 0 && d <= (u32)SD) {
                             own[k] = o;
                             yv[k] = s_head[j - j0];
                         }
@@ -183,48 +222,81 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             vy[k].d = 0;
             if (own[k] != NONE && yv[k] < n) vy[k] = load_desc(vdesc + yv[k]);
         }
-        u32 run_owner = NONE, run = 0;
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             const u32 o = own[k];
-            if (o == NONE) continue;
-            const u32 dx = s_desc[o].d;
-            const u32 y = yv[k];
-            const u32 dy = vy[k].d;
+            bool sel = false;
+            if (o != NONE) {
+                const u32 dy = vy[k].d;
+                sel = dy > 0 && key_less(dy, yv[k], s_desc[o].d, i0 + o);
+            }
+            const u32 ball = __ballot_sync(0xFFFFFFFFu, sel);
+            u32 base = 0;
+            if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (sel) {
+                const u32 qi = base + __popc(ball & ((1u << lane) - 1));
+                q_y[qi] = yv[k];
+                q_s[qi] = vy[k].start;
+                q_m[qi] = (o << 6) | vy[k].d;
+                atomicAdd(&s_bins[vy[k].d], 1u);
+            }
+        }
+        __syncthreads();
+
+        // counting sort of the queue by list length
+        const u32 qn = s_qn;
+        if (threadIdx.x < 32) {
+            u32 c0 = s_bins[lane], c1 = lane + 32 < SD + 2 ? s_bins[lane + 32] : 0;
+            u32 x0 = c0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                u32 y = __shfl_up_sync(0xFFFFFFFFu, x0, o);
+                if (lane >= o) x0 += y;
+            }
+            const u32 tot0 = __shfl_sync(0xFFFFFFFFu, x0, 31);
+            u32 x1 = c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                u32 y = __shfl_up_sync(0xFFFFFFFFu, x1, o);
+                if (lane >= o) x1 += y;
+            }
+            s_bins[lane] = x0 - c0;
+            if (lane + 32 < SD + 2) s_bins[lane + 32] = tot0 + x1 - c1;
+        }
+        __syncthreads();
+        for (u32 qi = threadIdx.x; qi < qn; qi += BLOCK) {
+            const u32 pos = atomicAdd(&s_bins[q_m[qi] & 63u], 1u);
+            q_ord[pos] = (unsigned short)qi;
+        }
+        __syncthreads();
+
+        // stream the queued lists (equal lengths side by side)
+        for (u32 r = threadIdx.x; r < qn; r += BLOCK) {
+            const u32 qi = q_ord[r];
+            const u32 meta = q_m[qi];
+            const u32 o = meta >> 6, dy = meta & 63u;
+            const u32 tb = s_tb[o];
+            const u32* keys = s_keys + (tb >> 5);
+            u32* hitc = s_hits + (tb >> 5);
+            const u32 lg = tb & 31u, shift = 32 - lg, mask = (1u << lg) - 1;
+            const u64 q0 = (u64)q_s[qi] >> 2;
             u32 hits = 0;
-            if (dy > 0 && key_less(dy, y, dx, i0 + o)) {
-                const u32 tb = s_tb[o];
-                u32* keys = s_keys + (tb >> 5);
-                u32* hitc = s_hits + (tb >> 5);
-                const u32 lg = tb & 31u;
-                const u64 q0 = (u64)vy[k].start >> 2;
 #pragma unroll
-                for (int c = 0; c < SD / 4; ++c) {
-                    if (4 * c < (int)dy) {
-                        const uint4 q = __ldg(headp4 + q0 + c);
-                        const u32 wv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            if (4 * c + e < (int)dy) {
-                                const u32 s = table_find(keys, lg, wv[e]);
-                                if (s != NONE) {
-                                    atomicAdd(&hitc[s], 1u);
-                                    ++hits;
-                                }
-                            }
-                        }
-                    }
+            for (int c = 0; c < SD / 4; ++c) {
+                if (4 * c < (int)dy) {
+                    const uint4 qv = __ldg(headp4 + q0 + c);
+                    hits += probe_hit(keys, hitc, shift, mask, qv.x);
+                    if (4 * c + 1 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.y);
+                    if (4 * c + 2 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.z);
+                    if (4 * c + 3 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.w);
                 }
             }
-            if (hits) atomicAdd(&cnt[y], (u64)hits);
-            if (o != run_owner) {
-                if (run) atomicAdd(&s_own[run_owner], run);
-                run_owner = o;
-                run = 0;
+            if (hits) {
+                atomicAdd(&cnt[q_y[qi]], (u64)hits);
+                atomicAdd(&s_own[o], hits);
             }
-            run += hits;
         }
-        if (run) atomicAdd(&s_own[run_owner], run);
         __syncthreads();
 
         // flush: hits of every key (vertex w), then the owners' own counts
@@ -248,12 +320,12 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
 
 template <int BLOCK, int CAP, typename OffT>
 struct LargeLayout {
-    static constexpr int TS = 2 * CAP;
+    static constexpr int TS = 2 * CAP;  // table slots (at most half full)
     static constexpr size_t off_keys = 0;
     static constexpr size_t off_hits = off_keys + sizeof(u32) * TS;
-    static constexpr size_t off_qd = off_hits + sizeof(u32) * TS;
-    static constexpr size_t off_qy = off_qd + sizeof(Desc<OffT>) * BLOCK;
-    static constexpr size_t bytes = off_qy + sizeof(u32) * BLOCK;
+    static constexpr size_t off_qy = off_hits + sizeof(u32) * TS;
+    static constexpr size_t off_qd = off_qy + sizeof(u32) * LARGE_SEG;
+    static constexpr size_t bytes = off_qd + sizeof(Desc<OffT>) * LARGE_SEG;
 };
 
 template <int BLOCK, int CAP, typename OffT>
@@ -267,11 +339,11 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     extern __shared__ __align__(16) unsigned char smem[];
     u32* keys = reinterpret_cast<u32*>(smem + L::off_keys);
     u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
-    Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
     u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
+    Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
     __shared__ u64 s_red[NW];
     __shared__ u64 s_t;
-    __shared__ u32 s_qn;
+    __shared__ u32 s_qn, s_next;
 
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -279,7 +351,6 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
     u64 local_total = 0;
     u32 dup = 0;
-    if (threadIdx.x == 0) s_qn = 0;
 
     while (true) {
         if (threadIdx.x == 0) s_t = atomicAdd(&ctl->large_next, 1ull);
@@ -296,12 +367,17 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         u64 T = 0;
         for (u32 c0 = 0; c0 < dx; c0 += CAP) {
             const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
-            u32 lg = ceil_log2(2 * klen);
+            u32 lg = ceil_log2(4 * klen);  // quarter full where the table has room
+            if (lg > 31 - __clz((u32)L::TS)) lg = 31 - __clz((u32)L::TS);
             if (lg < 1) lg = 1;
-            const u32 size = 1u << lg;
+            const u32 size = 1u << lg, mask = size - 1, shift = 32 - lg;
             for (u32 s = threadIdx.x; s < size; s += BLOCK) {
                 keys[s] = EMPTY_KEY;
                 hitc[s] = 0;
+            }
+            if (threadIdx.x == 0) {
+                s_qn = 0;
+                s_next = 0;
             }
             __syncthreads();
             for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
@@ -309,13 +385,16 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 if (!table_insert(keys, lg, w)) dup = 1;
             }
             __syncthreads();
-            for (u64 e0 = a; e0 < b; e0 += BLOCK) {
-                const u64 e = e0 + threadIdx.x;
+            // scan the segment: short lists now, long lists into the queue
+            for (u64 e0 = a + (u64)warp * 32; e0 < b; e0 += (u64)NW * 32) {
+                const u64 e = e0 + lane;
+                bool queue = false;
+                u32 y = 0;
+                Desc<OffT> vy;
+                vy.start = 0;
+                vy.d = 0;
                 if (e < b) {
-                    const u32 y = __ldg(head + e);
-                    Desc<OffT> vy;
-                    vy.start = 0;
-                    vy.d = 0;
+                    y = __ldg(head + e);
                     if (y < n) vy = load_desc(vdesc + y);
                     const u32 dy = vy.d;
                     if (dy > 0 && key_less(dy, y, dx, x)) {
@@ -326,17 +405,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                             for (int c = 0; c < LONG_LIST / 4; ++c) {
                                 if (4 * c < (int)dy) {
                                     const uint4 qv = __ldg(headp4 + q0 + c);
-                                    const u32 wv[4] = {qv.x, qv.y, qv.z, qv.w};
-#pragma unroll
-                                    for (int k = 0; k < 4; ++k) {
-                                        if (4 * c + k < (int)dy) {
-                                            const u32 s = table_find(keys, lg, wv[k]);
-                                            if (s != NONE) {
-                                                atomicAdd(&hitc[s], 1u);
-                                                ++hits;
-                                            }
-                                        }
-                                    }
+                                    hits += probe_hit(keys, hitc, shift, mask, qv.x);
+                                    if (4 * c + 1 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.y);
+                                    if (4 * c + 2 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.z);
+                                    if (4 * c + 3 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.w);
                                 }
                             }
                             if (hits) {
@@ -344,44 +416,44 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                                 T += hits;
                             }
                         } else {
-                            const u32 slot = atomicAdd(&s_qn, 1u);
-                            qd[slot] = vy;
-                            qy[slot] = y;
+                            queue = true;
                         }
                     }
                 }
-                __syncthreads();
-                const u32 nq = s_qn;
-                for (u32 qi = warp; qi < nq; qi += NW) {
-                    const Desc<OffT> vy = qd[qi];
-                    const u32 y = qy[qi];
-                    u32 hits = 0;
-                    const u64 q0 = (u64)vy.start >> 2;
-                    for (u32 p = 4 * lane; p < vy.d; p += 128) {
-                        const uint4 qv = __ldg(headp4 + q0 + (p >> 2));
-                        const u32 wv[4] = {qv.x, qv.y, qv.z, qv.w};
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            if (p + k < vy.d) {
-                                const u32 s = table_find(keys, lg, wv[k]);
-                                if (s != NONE) {
-                                    atomicAdd(&hitc[s], 1u);
-                                    ++hits;
-                                }
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) hits += __shfl_down_sync(0xFFFFFFFFu, hits, o);
-                    if (lane == 0 && hits) {
-                        atomicAdd(&cnt[y], (u64)hits);
-                        T += hits;
-                    }
+                const u32 ball = __ballot_sync(0xFFFFFFFFu, queue);
+                u32 base = 0;
+                if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (queue) {
+                    const u32 qi = base + __popc(ball & ((1u << lane) - 1));
+                    qy[qi] = y;
+                    qd[qi] = vy;
                 }
-                __syncthreads();
-                if (threadIdx.x == 0) s_qn = 0;
-                __syncthreads();
             }
+            __syncthreads();
+            // long lists: one warp per list, taken from the queue one at a time
+            const u32 qn = s_qn;
+            while (true) {
+                u32 qi = 0;
+                if (lane == 0) qi = atomicAdd(&s_next, 1u);
+                qi = __shfl_sync(0xFFFFFFFFu, qi, 0);
+                if (qi >= qn) break;
+                const Desc<OffT> vy = qd[qi];
+                const u32* lst = headp + (u64)vy.start;
+                u32 hits = 0;
+                for (u32 p = lane; p < vy.d; p += 64) {
+                    const u32 w0 = __ldg(lst + p);
+                    const u32 w1 = p + 32 < vy.d ? __ldg(lst + p + 32) : EMPTY_KEY;
+                    hits += probe_hit(keys, hitc, shift, mask, w0);
+                    if (w1 != EMPTY_KEY) hits += probe_hit(keys, hitc, shift, mask, w1);
+                }
+                hits = __reduce_add_sync(0xFFFFFFFFu, hits);
+                if (lane == 0 && hits) {
+                    atomicAdd(&cnt[qy[qi]], (u64)hits);
+                    T += hits;
+                }
+            }
+            __syncthreads();
             for (u32 s = threadIdx.x; s < size; s += BLOCK) {
                 const u32 h = hitc[s];
                 if (h) atomicAdd(&cnt[keys[s]], (u64)h);
@@ -492,13 +564,13 @@ int count_grid_large(int num_sms) {
 
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
+                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large) {
     const int gs = count_grid_small<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
     k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
-        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, cnt, partials, ctl);
+        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, cnt, partials, ctl);
     if (after_small) cudaEventRecord(after_small, st);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
         <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs, ctl);
@@ -522,9 +594,11 @@ template int count_grid_small<u32>(int);
 template int count_grid_small<u64>(int);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
-template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
+                                            const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
-template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
+                                            const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
 template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);

@@ -13,26 +13,32 @@ using u32 = uint32_t;
 using u64 = unsigned long long;
 
 constexpr int ORIENT_BLOCK = 256;
-constexpr int ORIENT_IPT = 8;
+constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
-constexpr int SMALL_IPT = 4;
+constexpr int SMALL_IPT = 3;
 constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
-constexpr int LARGE_BLOCK = 256;
-constexpr int LARGE_CAP = 4096;      // keys per shared-memory table chunk of the vertex kernel
+constexpr int LARGE_BLOCK = 512;
+constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of the vertex kernel
 constexpr u32 LARGE_SEG = 2048;      // adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
+// Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
+// the vertex where diagonal k * TILE_BASE crosses the path.  The counting tiles are one base
+// tile, the orientation tiles two.
+constexpr u64 TILE_BASE = 768;
+static_assert(ORIENT_BLOCK * ORIENT_IPT == 2 * TILE_BASE, "orientation tile = 2 base tiles");
+inline u64 base_tiles(u64 n, u64 nnz) { return (n + nnz + TILE_BASE - 1) / TILE_BASE; }
 inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d) {
     u64 owners = nnz / ((u64)small_d + 1) + 1;
     if (owners > n) owners = n;
     return owners + nnz / LARGE_SEG + 1;
 }
 
-void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, Control* ctl, int num_sms,
-                 cudaStream_t st);
-void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, u32* headp, u32* dplus,
-                   u32* spanning, Control* ctl, cudaStream_t st);
+void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
+                 int num_sms, cudaStream_t st);
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st);
 template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
                  Control* ctl, int num_sms, cudaStream_t st);
@@ -44,7 +50,7 @@ template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
+                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl, int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
 

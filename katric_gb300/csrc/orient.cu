@@ -15,26 +15,39 @@
 namespace ktri {
 
 // deg[v] = first_out[v+1] - first_out[v]; zero the out-degrees and the per-vertex counts.
+// Also tabulates the merge-path tile boundaries: vertex v covers the diagonals
+// [first_out[v] + v, first_out[v+1] + v] (its slots and its end event), so every boundary
+// k * TILE_BASE in that range crosses the path at vertex v.
 __global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restrict__ deg, u32* __restrict__ dplus,
-                       u64* __restrict__ cnt, Control* ctl) {
+                       u64* __restrict__ cnt, u32* __restrict__ tile_i0, Control* ctl) {
     const u64 stride = (u64)gridDim.x * blockDim.x;
+    const u64 nt = (n + nnz + TILE_BASE - 1) / TILE_BASE;
     u32 err = 0;
     for (u64 v = (u64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
         u64 a = fo[v], b = fo[v + 1];
         u32 d = 0;
-        if (b < a || b - a > 0xFFFFFFFFull || b > nnz) err |= DEV_ERR_DEGREE;
-        else d = (u32)(b - a);
+        if (b < a || b - a > 0xFFFFFFFFull || b > nnz) {
+            err |= DEV_ERR_DEGREE;
+        } else {
+            d = (u32)(b - a);
+            const u64 k0 = (a + v + TILE_BASE - 1) / TILE_BASE, k1 = (b + v) / TILE_BASE;
+            for (u64 k = k0; k <= k1 && k < nt; ++k) tile_i0[k] = (u32)v;
+        }
         deg[v] = d;
         dplus[v] = 0;
         if (cnt) cnt[v] = 0;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && (fo[0] != 0 || fo[n] != nnz)) err |= DEV_ERR_DEGREE;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        tile_i0[nt] = (u32)n;
+        if (fo[0] != 0 || fo[n] != nnz) err |= DEV_ERR_DEGREE;
+    }
     if (err) atomicOr(&ctl->err, err);
 }
 
 template <int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
-                                                  u64 nnz, const u32* __restrict__ deg, u32* __restrict__ headp,
+                                                  u64 nnz, const u32* __restrict__ deg,
+                                                  const u32* __restrict__ tile_i0, u32* __restrict__ headp,
                                                   u32* __restrict__ dplus, u32* __restrict__ spanning,
                                                   Control* ctl) {
     constexpr int TILE = BLOCK * IPT;
@@ -51,8 +64,12 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     const u64 d0 = (u64)blockIdx.x * TILE;
     if (d0 >= total) return;
     const u64 d1 = d0 + TILE < total ? d0 + TILE : total;
-    if (threadIdx.x == 0) s_b[0] = mp_search(fo, n, d0);
-    if (threadIdx.x == 32) s_b[1] = mp_search(fo, n, d1);
+    if (threadIdx.x == 0) {
+        const u64 nt = (total + TILE_BASE - 1) / TILE_BASE;
+        const u64 k1 = 2 * (u64)blockIdx.x + 2;
+        s_b[0] = tile_i0[2 * (u64)blockIdx.x];
+        s_b[1] = tile_i0[k1 < nt ? k1 : nt];
+    }
     __syncthreads();
     const u64 i0 = s_b[0], i1 = s_b[1];
     const u64 j0 = d0 - i0, j1 = d1 - i1;
@@ -225,21 +242,22 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
 
 // ---- launchers ------------------------------------------------------------------------
 
-void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, Control* ctl, int num_sms,
-                 cudaStream_t st) {
+void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
+                 int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u64 blocks = (n + 255) / 256;
     u64 cap = (u64)num_sms * 8;
-    k_prep<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(fo, n, nnz, deg, dplus, cnt, ctl);
+    k_prep<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl);
 }
 
-void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, u32* headp, u32* dplus,
-                   u32* spanning, Control* ctl, cudaStream_t st) {
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st) {
     constexpr int BLOCK = ORIENT_BLOCK, IPT = ORIENT_IPT;
     const u64 total = n + nnz;
     if (total == 0) return;
     const u64 tiles = (total + BLOCK * IPT - 1) / (BLOCK * IPT);
-    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, headp, dplus, spanning, ctl);
+    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning,
+                                                             ctl);
 }
 
 template <typename OffT>
