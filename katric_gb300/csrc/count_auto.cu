@@ -27,41 +27,25 @@
 
 namespace ktri {
 
-// Probe key w in the open-addressing table keys[0, mask] (linear probing, multiplicative
-// hash, 32-lg = shift).  On a hit, count it in the slot's counter.  Tables are at most half
-// full, so an empty slot ends every miss.
-__device__ __forceinline__ u32 probe_hit(const u32* keys, u32* hits, u32 shift, u32 mask, u32 w) {
-    u32 s = (w * 0x9E3779B1u) >> shift;
-    for (u32 it = 0; it <= mask; ++it) {
-        const u32 k = keys[s];
-        if (k == w) {
-            atomicAdd(&hits[s], 1u);
-            return 1u;
-        }
-        if (k == EMPTY_KEY) return 0u;
-        s = (s + 1) & mask;
-    }
-    return 0u;
-}
+constexpr size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 template <int BLOCK, int IPT, int SD, typename OffT>
 struct SmallLayout {
     static constexpr int TILE = BLOCK * IPT;
-    static constexpr int TBL = 4 * (TILE + 2 * SD);  // sum of per-owner table sizes (pow2 >= 2 d <= 4 d)
+    static constexpr int TBL = 4 * (TILE + 2 * SD);  // sum of per-owner table sizes (pow2 >= max(4, 2d) <= 4d)
     static constexpr int WPT = (TILE + 1 + BLOCK - 1) / BLOCK;
-    static constexpr size_t off_fo = 0;
-    static constexpr size_t off_desc = off_fo + sizeof(u64) * (TILE + 2);
-    static constexpr size_t off_head = off_desc + sizeof(Desc<OffT>) * (TILE + 2);
-    static constexpr size_t off_tb = off_head + sizeof(u32) * TILE;
-    static constexpr size_t off_ko = off_tb + sizeof(u32) * (TILE + 2);
-    static constexpr size_t off_own = off_ko + sizeof(u32) * (TILE + 2);
-    static constexpr size_t off_keys = off_own + sizeof(u32) * (TILE + 2);
-    static constexpr size_t off_hits = off_keys + sizeof(u32) * TBL;
-    static constexpr size_t off_qy = off_hits + sizeof(u32) * TBL;
-    static constexpr size_t off_qs = off_qy + sizeof(u32) * TILE;
-    static constexpr size_t off_qm = off_qs + sizeof(OffT) * TILE;
-    static constexpr size_t off_ord = off_qm + sizeof(u32) * TILE;
-    static constexpr size_t bytes = off_ord + sizeof(unsigned short) * TILE;
+    static constexpr size_t off_fo = 0;  // first_out of the window, clamped to the tile, relative to its first slot
+    static constexpr size_t off_desc = align16(off_fo + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_tb = align16(off_desc + sizeof(Desc<OffT>) * (TILE + 2));
+    static constexpr size_t off_ko = align16(off_tb + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_own = align16(off_ko + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_keys = align16(off_own + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TBL);
+    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * TBL);
+    static constexpr size_t off_qs = align16(off_qy + sizeof(u32) * TILE);
+    static constexpr size_t off_qm = align16(off_qs + sizeof(OffT) * TILE);
+    static constexpr size_t off_ord = align16(off_qm + sizeof(u32) * TILE);
+    static constexpr size_t bytes = align16(off_ord + sizeof(unsigned short) * TILE);
 };
 
 template <int BLOCK, int IPT, int SD, typename OffT>
@@ -76,9 +60,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
     constexpr int WPT = L::WPT;
     static_assert(SD < 64, "list length is packed in 6 bits");
     extern __shared__ __align__(16) unsigned char smem[];
-    u64* s_fo = reinterpret_cast<u64*>(smem + L::off_fo);
+    u32* s_fo = reinterpret_cast<u32*>(smem + L::off_fo);
     Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
-    u32* s_head = reinterpret_cast<u32*>(smem + L::off_head);
     u32* s_tb = reinterpret_cast<u32*>(smem + L::off_tb);
     u32* s_ko = reinterpret_cast<u32*>(smem + L::off_ko);
     u32* s_own = reinterpret_cast<u32*>(smem + L::off_own);
@@ -124,13 +107,15 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         const u64 j0 = d0 - i0, j1 = d1 - i1;
         const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
         const u32 nw = (u32)(fo_last - i0);  // window vertices [i0, fo_last)
-        for (u32 k = threadIdx.x; k <= nw; k += BLOCK) s_fo[k] = fo[i0 + k];
+        for (u32 k = threadIdx.x; k <= nw; k += BLOCK) {
+            u64 f = fo[i0 + k];
+            f = f < j0 ? j0 : (f > j1 ? j1 : f);
+            s_fo[k] = (u32)(f - j0);
+        }
         for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
             s_desc[k] = load_desc(vdesc + i0 + k);
             s_own[k] = 0;
         }
-        const u32 nslot = (u32)(j1 - j0);
-        for (u32 k = threadIdx.x; k < nslot; k += BLOCK) s_head[k] = head[j0 + k];
         __syncthreads();
 
         // table sizes and key offsets of the owners in the window
@@ -141,12 +126,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             const u32 k = threadIdx.x * WPT + r;
             packed[r] = 0;
             if (k < nw) {
-                const u64 a = s_fo[k], b = s_fo[k + 1];
-                const u64 lo = a > j0 ? a : j0, hi = b < j1 ? b : j1;
                 const u32 d = s_desc[k].d;
-                if (lo < hi && d > 0 && d <= (u32)SD) {
+                if (s_fo[k] < s_fo[k + 1] && d > 0 && d <= (u32)SD) {
                     u32 lg = ceil_log2(2 * d);
-                    if (lg < 1) lg = 1;
+                    if (lg < 2) lg = 2;
                     packed[r] = ((1u << lg) << 16) | d;
                 }
             }
@@ -186,16 +169,26 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             }
             const u32 tb = s_tb[lo];
             const u32 w = __ldg(headp + (u64)s_desc[lo].start + (q - s_ko[lo]));
-            if (!table_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
+            if (!bucket_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
         }
 
         // walk this thread's items of the merge path and queue the edges this tile owns
         const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
         const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
-        const u64 i_start = mp_search_window(s_fo, i0, i0, i1, dt);
+        // merge-path search in the window: largest i in [i0, i1] with first_out[i] + i <= dt
+        u64 i_start;
+        {
+            u64 lo = i0, hi = i1;
+            while (lo < hi) {
+                const u64 mid = (lo + hi + 1) >> 1;
+                if ((u64)s_fo[mid - i0] + j0 + mid <= dt) lo = mid; else hi = mid - 1;
+            }
+            i_start = lo;
+        }
         u32 own[IPT], yv[IPT];
         {
-            u64 i = i_start, j = dt - i_start;
+            u64 i = i_start;
+            u32 j = (u32)(dt - i_start - j0);  // slot relative to the tile's first slot
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
                 own[k] = NONE;
@@ -206,7 +199,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
                         const u32 d = s_desc[o].d;
                         if (d > 0 && d <= (u32)SD) {
                             own[k] = o;
-                            yv[k] = s_head[j - j0];
+                            yv[k] = __ldg(head + j0 + j);
                         }
                         ++j;
                     } else {
@@ -279,17 +272,17 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             const u32 tb = s_tb[o];
             const u32* keys = s_keys + (tb >> 5);
             u32* hitc = s_hits + (tb >> 5);
-            const u32 lg = tb & 31u, shift = 32 - lg, mask = (1u << lg) - 1;
+            const u32 lg = tb & 31u;
             const u64 q0 = (u64)q_s[qi] >> 2;
             u32 hits = 0;
 #pragma unroll
             for (int c = 0; c < SD / 4; ++c) {
                 if (4 * c < (int)dy) {
                     const uint4 qv = __ldg(headp4 + q0 + c);
-                    hits += probe_hit(keys, hitc, shift, mask, qv.x);
-                    if (4 * c + 1 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.y);
-                    if (4 * c + 2 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.z);
-                    if (4 * c + 3 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.w);
+                    hits += bucket_probe(keys, hitc, lg, qv.x);
+                    if (4 * c + 1 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.y);
+                    if (4 * c + 2 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.z);
+                    if (4 * c + 3 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.w);
                 }
             }
             if (hits) {
@@ -322,10 +315,10 @@ template <int BLOCK, int CAP, typename OffT>
 struct LargeLayout {
     static constexpr int TS = 2 * CAP;  // table slots (at most half full)
     static constexpr size_t off_keys = 0;
-    static constexpr size_t off_hits = off_keys + sizeof(u32) * TS;
-    static constexpr size_t off_qy = off_hits + sizeof(u32) * TS;
-    static constexpr size_t off_qd = off_qy + sizeof(u32) * LARGE_SEG;
-    static constexpr size_t bytes = off_qd + sizeof(Desc<OffT>) * LARGE_SEG;
+    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TS);
+    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * TS);
+    static constexpr size_t off_qd = align16(off_qy + sizeof(u32) * LARGE_SEG);
+    static constexpr size_t bytes = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
 };
 
 template <int BLOCK, int CAP, typename OffT>
@@ -369,8 +362,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
             u32 lg = ceil_log2(4 * klen);  // quarter full where the table has room
             if (lg > 31 - __clz((u32)L::TS)) lg = 31 - __clz((u32)L::TS);
-            if (lg < 1) lg = 1;
-            const u32 size = 1u << lg, mask = size - 1, shift = 32 - lg;
+            if (lg < 2) lg = 2;
+            const u32 size = 1u << lg;
             for (u32 s = threadIdx.x; s < size; s += BLOCK) {
                 keys[s] = EMPTY_KEY;
                 hitc[s] = 0;
@@ -382,7 +375,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             __syncthreads();
             for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
                 const u32 w = __ldg(headp + (u64)dxd.start + c0 + q);
-                if (!table_insert(keys, lg, w)) dup = 1;
+                if (!bucket_insert(keys, lg, w)) dup = 1;
             }
             __syncthreads();
             // scan the segment: short lists now, long lists into the queue
@@ -405,10 +398,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                             for (int c = 0; c < LONG_LIST / 4; ++c) {
                                 if (4 * c < (int)dy) {
                                     const uint4 qv = __ldg(headp4 + q0 + c);
-                                    hits += probe_hit(keys, hitc, shift, mask, qv.x);
-                                    if (4 * c + 1 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.y);
-                                    if (4 * c + 2 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.z);
-                                    if (4 * c + 3 < (int)dy) hits += probe_hit(keys, hitc, shift, mask, qv.w);
+                                    hits += bucket_probe(keys, hitc, lg, qv.x);
+                                    if (4 * c + 1 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.y);
+                                    if (4 * c + 2 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.z);
+                                    if (4 * c + 3 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.w);
                                 }
                             }
                             if (hits) {
@@ -444,8 +437,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 for (u32 p = lane; p < vy.d; p += 64) {
                     const u32 w0 = __ldg(lst + p);
                     const u32 w1 = p + 32 < vy.d ? __ldg(lst + p + 32) : EMPTY_KEY;
-                    hits += probe_hit(keys, hitc, shift, mask, w0);
-                    if (w1 != EMPTY_KEY) hits += probe_hit(keys, hitc, shift, mask, w1);
+                    hits += bucket_probe(keys, hitc, lg, w0);
+                    if (w1 != EMPTY_KEY) hits += bucket_probe(keys, hitc, lg, w1);
                 }
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
                 if (lane == 0 && hits) {

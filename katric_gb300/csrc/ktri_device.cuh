@@ -156,6 +156,49 @@ __device__ __forceinline__ u32 table_find(const u32* keys, u32 lg, u32 w) {
     return NONE;
 }
 
+// Bucketized open addressing for the counting tables: 2^lg slots (lg >= 2) in buckets of
+// four.  A key hashes to a bucket; inserts fill a bucket's slots in order (slot i is taken
+// only after slots 0..i-1), so a bucket whose last slot is empty ends every lookup.  A lookup
+// reads one bucket (16 bytes) per step; at the load factors used here almost every lookup
+// ends in its first bucket, which keeps the lanes of a warp in step.
+__device__ __forceinline__ u32 bucket_home(u32 w, u32 lg) {
+    return lg > 2 ? ((w * 0x9E3779B1u) >> (34 - lg)) : 0u;
+}
+
+// Returns false when w was already present.
+__device__ __forceinline__ bool bucket_insert(u32* keys, u32 lg, u32 w) {
+    const u32 nb_mask = (1u << (lg - 2)) - 1;
+    u32 b = bucket_home(w, lg);
+    for (u32 it = 0; it <= nb_mask; ++it) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const u32 prev = atomicCAS(&keys[4 * b + i], EMPTY_KEY, w);
+            if (prev == EMPTY_KEY) return true;
+            if (prev == w) return false;
+        }
+        b = (b + 1) & nb_mask;
+    }
+    return true;  // unreachable: tables are at most half full
+}
+
+// Count a lookup of w: on a hit, add one to the slot's hit counter and return 1.
+__device__ __forceinline__ u32 bucket_probe(const u32* keys, u32* hits, u32 lg, u32 w) {
+    const u32 nb_mask = (1u << (lg - 2)) - 1;
+    u32 b = bucket_home(w, lg);
+    for (u32 it = 0; it <= nb_mask; ++it) {
+        const uint4 q = *reinterpret_cast<const uint4*>(keys + 4 * b);
+        const bool m0 = q.x == w, m1 = q.y == w, m2 = q.z == w, m3 = q.w == w;
+        if (m0 | m1 | m2 | m3) {
+            const u32 i = m0 ? 0u : (m1 ? 1u : (m2 ? 2u : 3u));
+            atomicAdd(&hits[4 * b + i], 1u);
+            return 1u;
+        }
+        if (q.w == EMPTY_KEY) return 0u;
+        b = (b + 1) & nb_mask;
+    }
+    return 0u;
+}
+
 __host__ __device__ __forceinline__ u32 ceil_log2(u32 v) {
     u32 lg = 0;
     while ((1u << lg) < v) ++lg;

@@ -17,9 +17,9 @@ constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
 constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
-constexpr int LARGE_BLOCK = 512;
+constexpr int LARGE_BLOCK = 256;
 constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of the vertex kernel
-constexpr u32 LARGE_SEG = 2048;      // adjacency slots per (owner, segment) tile
+constexpr u32 LARGE_SEG = 1024;      // adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
