@@ -44,7 +44,7 @@ constexpr size_t ALIGN = 256;
 inline size_t align_up(size_t x) { return (x + ALIGN - 1) & ~(ALIGN - 1); }
 
 struct Layout {
-    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, core_idx = 0, core_inv = 0, vdesc = 0, headp = 0, ltiles = 0, spanning = 0, partials = 0, cnt = 0,
+    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, vdesc = 0, headp = 0, ltiles = 0, spanning = 0, partials = 0, cnt = 0,
            total = 0, mid = 0, big = 0, scratch = 0, in_fo = 0, in_head = 0, bytes = 0;
     bool wide = false;
     u64 scratch_per_block = 0;
@@ -81,8 +81,6 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
         L.ltiles = take(sizeof(uint2) * ktri::large_tile_capacity(n, nnz, ktri::SMALL_D));
-        L.core_idx = take(sizeof(u32) * (n + 1));
-        L.core_inv = take(sizeof(u32) * ktri::CORE_MAX);
         grid = (u32)(sms * 16);  // bound on small + large persistent grids (occupancy <= 8 each)
     } else {
         L.mid = take(sizeof(u32) * (n + 1));
@@ -193,11 +191,8 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
     KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
     KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
     const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
-    auto* core_idx = autom ? reinterpret_cast<u32*>(base + L.core_idx) : nullptr;
-    auto* core_inv = autom ? reinterpret_cast<u32*>(base + L.core_inv) : nullptr;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
-    if (autom) ktri::launch_core(n, deg, core_idx, core_inv, ctl, sms, st);
-    ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, core_idx, headp, dplus, spanning, ctl, st);
+    ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
     auto* ltiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, ltiles, autom ? (u32)ktri::SMALL_D : 0xFFFFFFFFu,
                             ktri::LARGE_SEG, ctl, sms, st);
@@ -207,13 +202,12 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
                                       L.scratch_per_block, L.big_grid, ctl, sms, st);
     }
     KTRI_CK(ctx, cudaEventRecord(ctx->ev[1], st));
-    if (opt.collect_stats) ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, core_inv, ctl, sms, st);
+    if (opt.collect_stats) ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, ctl, sms, st);
     KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, core_inv, cnt, partials, ctl, sms,
-                                                   st,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl, sms, st,
                                                    ctx->ev[4], ctx->ev[5]));
         const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
         ktri::launch_final(partials, np, d_total, ctl, st);

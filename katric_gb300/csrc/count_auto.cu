@@ -21,7 +21,7 @@
 //   k_count_large: owners above SMALL_D, one (owner, segment of LARGE_SEG slots) tile per
 //     block iteration.  Short streamed lists are handled one per thread while the segment is
 //     scanned; longer ones are queued and taken one at a time by whole warps (one entry per
-//     lane, two loads in flight), so no block-wide barrier separates the lists.
+//     lane, eight loads in flight), so no block-wide barrier separates the lists.
 #include "ktri_device.cuh"
 #include "ktri_kernels.h"
 
@@ -52,8 +52,7 @@ template <int BLOCK, int IPT, int SD, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
                                                        const u32* __restrict__ headp,
-                                                       const u32* __restrict__ tile_i0,
-                                                       const u32* __restrict__ core_inv, u64* __restrict__ cnt,
+                                                       const u32* __restrict__ tile_i0, u64* __restrict__ cnt,
                                                        u64* __restrict__ partials, Control* ctl) {
     using L = SmallLayout<BLOCK, IPT, SD, OffT>;
     static_assert(L::TILE == TILE_BASE, "one counting tile = one base tile");
@@ -296,7 +295,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         // flush: hits of every key (vertex w), then the owners' own counts
         for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
             const u32 h = s_hits[s];
-            if (h) atomicAdd(&cnt[label_vertex(s_keys[s], core_inv)], (u64)h);
+            if (h) atomicAdd(&cnt[s_keys[s]], (u64)h);
         }
         for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
             const u32 t = s_own[k];
@@ -319,26 +318,14 @@ struct LargeLayout {
     static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TS);
     static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * TS);
     static constexpr size_t off_qd = align16(off_qy + sizeof(u32) * LARGE_SEG);
-    static constexpr size_t off_bm = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);  // core bitmap
-    static constexpr size_t bytes = align16(off_bm + sizeof(u32) * (CORE_MAX / 32));
+    static constexpr size_t bytes = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
 };
-
-// Lookup of label w against the owner's table, with the core bitmap in front: a core label
-// whose bit is clear is a miss after one shared-memory word test.
-__device__ __forceinline__ u32 core_probe(const u32* bm, const u32* keys, u32* hits, u32 lg, u32 w) {
-    if (w & CORE_TAG) {
-        const u32 c = w & 0x7FFFFFFFu;
-        if (!((bm[c >> 5] >> (c & 31)) & 1u)) return 0u;
-    }
-    return bucket_probe(keys, hits, lg, w);
-}
 
 template <int BLOCK, int CAP, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, const Desc<OffT>* __restrict__ vdesc,
                                                        const u32* __restrict__ headp,
-                                                       const uint2* __restrict__ ltiles,
-                                                       const u32* __restrict__ core_inv, u64* __restrict__ cnt,
+                                                       const uint2* __restrict__ ltiles, u64* __restrict__ cnt,
                                                        u64* __restrict__ partials, Control* ctl) {
     using L = LargeLayout<BLOCK, CAP, OffT>;
     constexpr int NW = BLOCK / 32;
@@ -348,7 +335,6 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
     u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
     Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
-    u32* bm = reinterpret_cast<u32*>(smem + L::off_bm);
     __shared__ u64 s_red[NW];
     __shared__ u64 s_t;
     __shared__ u32 s_qn, s_next;
@@ -359,7 +345,6 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
     u64 local_total = 0;
     u32 dup = 0;
-    for (u32 i = threadIdx.x; i < CORE_MAX / 32; i += BLOCK) bm[i] = 0;
 
     while (true) {
         if (threadIdx.x == 0) s_t = atomicAdd(&ctl->large_next, 1ull);
@@ -392,10 +377,6 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
                 const u32 w = __ldg(headp + (u64)dxd.start + c0 + q);
                 if (!bucket_insert(keys, lg, w)) dup = 1;
-                if (w & CORE_TAG) {
-                    const u32 c = w & 0x7FFFFFFFu;
-                    atomicOr(&bm[c >> 5], 1u << (c & 31));
-                }
             }
             __syncthreads();
             // scan the segment: short lists now, long lists into the queue
@@ -422,10 +403,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
 #pragma unroll
                             for (int c = 0; c < LONG_LIST / 4; ++c) {
                                 if (4 * c < (int)dy) {
-                                    hits += core_probe(bm, keys, hitc, lg, qv[c].x);
-                                    if (4 * c + 1 < (int)dy) hits += core_probe(bm, keys, hitc, lg, qv[c].y);
-                                    if (4 * c + 2 < (int)dy) hits += core_probe(bm, keys, hitc, lg, qv[c].z);
-                                    if (4 * c + 3 < (int)dy) hits += core_probe(bm, keys, hitc, lg, qv[c].w);
+                                    hits += bucket_probe(keys, hitc, lg, qv[c].x);
+                                    if (4 * c + 1 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].y);
+                                    if (4 * c + 2 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].z);
+                                    if (4 * c + 3 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].w);
                                 }
                             }
                             if (hits) {
@@ -467,7 +448,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                     }
 #pragma unroll
                     for (int u = 0; u < U; ++u)
-                        if (w[u] != EMPTY_KEY) hits += core_probe(bm, keys, hitc, lg, w[u]);
+                        if (w[u] != EMPTY_KEY) hits += bucket_probe(keys, hitc, lg, w[u]);
                 }
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
                 if (lane == 0 && hits) {
@@ -476,14 +457,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 }
             }
             __syncthreads();
-            // flush the hits of every key, and clear the core bits this chunk set
+            // flush the hits of every key
             for (u32 s = threadIdx.x; s < size; s += BLOCK) {
-                const u32 k = keys[s];
-                if (k != EMPTY_KEY) {
-                    const u32 h = hitc[s];
-                    if (h) atomicAdd(&cnt[label_vertex(k, core_inv)], (u64)h);
-                    if (k & CORE_TAG) bm[(k & 0x7FFFFFFFu) >> 5] = 0;
-                }
+                const u32 h = hitc[s];
+                if (h) atomicAdd(&cnt[keys[s]], (u64)h);
             }
             __syncthreads();
         }
@@ -510,8 +487,7 @@ __global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials
 // (cetric_edge_iterator.h:279-281), plus the entries streamed by the AUTO kernels.
 template <typename OffT>
 __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
-                        const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp,
-                        const u32* __restrict__ core_inv, Control* ctl) {
+                        const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
     const u64 gw = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -521,7 +497,7 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
         const Desc<OffT> dv = load_desc(vdesc + v);
         if (lane == 0) oriented += dv.d;
         for (u32 k = lane; k < dv.d; k += 32) {
-            const u32 u = core_inv ? label_vertex(headp[(u64)dv.start + k], core_inv) : headp[(u64)dv.start + k];
+            const u32 u = headp[(u64)dv.start + k];
             const u32 du = load_desc(vdesc + u).d;
             wedge += du;
             isz += (u64)dv.d + du;
@@ -592,17 +568,17 @@ int count_grid_large(int num_sms) {
 
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* ltiles, const u32* core_inv, u64* cnt, u64* partials,
-                              Control* ctl, int num_sms,
+                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl,
+                              int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large) {
     const int gs = count_grid_small<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
     k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
-        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, core_inv, cnt, partials, ctl);
+        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, cnt, partials, ctl);
     if (after_small) cudaEventRecord(after_small, st);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
-        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, core_inv, cnt, partials + gs, ctl);
+        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs, ctl);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
 }
@@ -613,11 +589,10 @@ void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStr
 }
 
 template <typename OffT>
-void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, const u32* core_inv,
-                  Control* ctl, int num_sms, cudaStream_t st) {
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
+                  int num_sms, cudaStream_t st) {
     if (n == 0) return;
-    k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp,
-                                               core_inv, ctl);
+    k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp, ctl);
 }
 
 template int count_grid_small<u32>(int);
@@ -625,14 +600,12 @@ template int count_grid_small<u64>(int);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
 template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const u32*,
+                                            const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const u32*,
+                                            const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
-template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, const u32*, Control*, int,
-                                cudaStream_t);
-template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, const u32*, Control*, int,
-                                cudaStream_t);
+template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
+template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
 
 }  // namespace ktri

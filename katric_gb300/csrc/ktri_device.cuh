@@ -156,12 +156,6 @@ __device__ __forceinline__ u32 table_find(const u32* keys, u32 lg, u32 w) {
     return NONE;
 }
 
-// Out-list entries of the AUTO path are labels: a vertex id, or CORE_TAG | core index for
-// the vertices of the core (see ktri_kernels.h).  core_inv maps a core index back.
-__device__ __forceinline__ u32 label_vertex(u32 label, const u32* __restrict__ core_inv) {
-    return (label & 0x80000000u) ? __ldg(core_inv + (label & 0x7FFFFFFFu)) : label;
-}
-
 // Bucketized open addressing for the counting tables: 2^lg slots (lg >= 2) in buckets of
 // four.  A key hashes to a bucket; inserts fill a bucket's slots in order (slot i is taken
 // only after slots 0..i-1), so a bucket whose last slot is empty ends every lookup.  A lookup

@@ -48,9 +48,7 @@ struct Control {
     unsigned long long stat_oriented;    // collect_stats: sum of out-degrees
     unsigned long long sort_mid;         // lists sorted by whole blocks in shared memory
     unsigned long long sort_big;         // lists sorted by whole blocks in global scratch
-    unsigned long long core_count;       // vertices given a core index
-    unsigned long long pad[3];
-    uint32_t class_count[34];            // vertices per degree class floor(log2(deg)) + 1 (class 0: deg 0)
+    unsigned long long pad[4];
 };
 
 }  // namespace ktri

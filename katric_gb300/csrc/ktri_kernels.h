@@ -17,17 +17,10 @@ constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
 constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
-constexpr int LARGE_BLOCK = 512;
+constexpr int LARGE_BLOCK = 256;
 constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of the vertex kernel
 constexpr u32 LARGE_SEG = 1024;      // adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
-// Core relabelling (KTRI_METHOD_AUTO): the vertices of the highest degree classes, up to
-// CORE_MAX of them, get dense core indices; out-lists store them as CORE_TAG | index.  On
-// skewed graphs nearly every probe of the large-owner kernel lands in the core, where a
-// shared-memory bitmap answers it with one bit test.
-constexpr u32 CORE_MAX = 1u << 19;
-constexpr u32 CORE_TAG = 0x80000000u;
-constexpr u32 CORE_MIN_DEGREE = 16;  // vertices below this degree never join the core
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
 // Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
@@ -44,9 +37,8 @@ inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d) {
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
                  int num_sms, cudaStream_t st);
-void launch_core(u64 n, const u32* deg, u32* core_idx, u32* core_inv, Control* ctl, int num_sms, cudaStream_t st);
-void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0,
-                   const u32* core_idx, u32* headp, u32* dplus, u32* spanning, Control* ctl, cudaStream_t st);
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st);
 template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
                  Control* ctl, int num_sms, cudaStream_t st);
@@ -58,16 +50,16 @@ template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* ltiles, const u32* core_inv, u64* cnt, u64* partials,
-                              Control* ctl, int num_sms,
+                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl,
+                              int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
 
 // Work counters of the reference (wedge_checks, intersection_size_local) and of the AUTO
 // kernels, accumulated into the control block.
 template <typename OffT>
-void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, const u32* core_inv,
-                  Control* ctl, int num_sms, cudaStream_t st);
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
+                  int num_sms, cudaStream_t st);
 
 // Sorted-list strategies (merge, binary search, binary, hybrid): sort out-lists by id, then
 // one warp per oriented edge.

@@ -20,11 +20,8 @@ namespace ktri {
 // k * TILE_BASE in that range crosses the path at vertex v.
 __global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restrict__ deg, u32* __restrict__ dplus,
                        u64* __restrict__ cnt, u32* __restrict__ tile_i0, Control* ctl) {
-    __shared__ u32 s_cls[34];
     const u64 stride = (u64)gridDim.x * blockDim.x;
     const u64 nt = (n + nnz + TILE_BASE - 1) / TILE_BASE;
-    if (threadIdx.x < 34) s_cls[threadIdx.x] = 0;
-    __syncthreads();
     u32 err = 0;
     for (u64 v = (u64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
         u64 a = fo[v], b = fo[v + 1];
@@ -39,65 +36,18 @@ __global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restri
         deg[v] = d;
         dplus[v] = 0;
         if (cnt) cnt[v] = 0;
-        atomicAdd(&s_cls[32 - __clz(d)], 1u);  // degree class: floor(log2 d) + 1, 0 for d = 0
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         tile_i0[nt] = (u32)n;
         if (fo[0] != 0 || fo[n] != nnz) err |= DEV_ERR_DEGREE;
     }
     if (err) atomicOr(&ctl->err, err);
-    __syncthreads();
-    if (threadIdx.x < 34 && s_cls[threadIdx.x]) atomicAdd(&ctl->class_count[threadIdx.x], s_cls[threadIdx.x]);
-}
-
-// Core relabelling: the vertices of the highest degree classes (at most CORE_MAX of them,
-// none below CORE_MIN_DEGREE) get dense core indices in any order.  Counts do not depend on
-// the order; it only decides where a vertex's bit sits in the counting kernels' bitmaps.
-__global__ void k_core(u64 n, const u32* __restrict__ deg, u32* __restrict__ core_idx, u32* __restrict__ core_inv,
-                       Control* ctl) {
-    __shared__ u32 s_tau;
-    if (ctl->err & DEV_ERR_MASK) return;
-    if (threadIdx.x == 0) {
-        u64 acc = 0;
-        u32 tau = 34;
-        for (int c = 33; c >= 1; --c) {
-            acc += ctl->class_count[c];
-            if (acc > CORE_MAX) break;
-            tau = (u32)c;
-        }
-        const u32 minc = 32 - __clz(CORE_MIN_DEGREE);
-        if (tau < minc) tau = minc;
-        if (n >= (1ull << 31)) tau = 34;  // labels need the top id bit free
-        s_tau = tau;
-    }
-    __syncthreads();
-    const u32 tau = s_tau;
-    const int lane = threadIdx.x & 31;
-    const u64 gw = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
-    for (u64 base = gw * 32; base < n; base += nwarps * 32) {
-        const u64 v = base + lane;
-        const bool in = v < n && (32 - __clz(deg[v])) >= tau;
-        const u32 ball = __ballot_sync(0xFFFFFFFFu, in);
-        u64 wbase = 0;
-        if (lane == 0 && ball) wbase = atomicAdd(&ctl->core_count, (u64)__popc(ball));
-        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-        if (v < n) {
-            u32 c = NONE;
-            if (in) {
-                c = (u32)(wbase + __popc(ball & ((1u << lane) - 1)));
-                core_inv[c] = (u32)v;
-            }
-            core_idx[v] = c;
-        }
-    }
 }
 
 template <int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
                                                   u64 nnz, const u32* __restrict__ deg,
-                                                  const u32* __restrict__ tile_i0,
-                                                  const u32* __restrict__ core_idx, u32* __restrict__ headp,
+                                                  const u32* __restrict__ tile_i0, u32* __restrict__ headp,
                                                   u32* __restrict__ dplus, u32* __restrict__ spanning,
                                                   Control* ctl) {
     constexpr int TILE = BLOCK * IPT;
@@ -246,12 +196,7 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
             const u64 x = i0 + o;
             const u32 carry = (x == i0) ? s_carry[0] : (x == i1 ? s_carry[1] : 0u);
             const u64 pos = (u64)(run - s_first[o]) + carry;
-            u32 label = yv[k];
-            if (core_idx) {
-                const u32 c = __ldg(core_idx + label);
-                if (c != NONE) label = CORE_TAG | c;
-            }
-            headp[oriented_start(s_fo[o], x) + pos] = label;
+            headp[oriented_start(s_fo[o], x) + pos] = yv[k];
             ++run;
         }
     }
@@ -305,21 +250,14 @@ void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, 
     k_prep<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl);
 }
 
-void launch_core(u64 n, const u32* deg, u32* core_idx, u32* core_inv, Control* ctl, int num_sms, cudaStream_t st) {
-    if (n == 0) return;
-    u64 blocks = (n + 255) / 256;
-    u64 cap = (u64)num_sms * 8;
-    k_core<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(n, deg, core_idx, core_inv, ctl);
-}
-
-void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0,
-                   const u32* core_idx, u32* headp, u32* dplus, u32* spanning, Control* ctl, cudaStream_t st) {
+void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st) {
     constexpr int BLOCK = ORIENT_BLOCK, IPT = ORIENT_IPT;
     const u64 total = n + nnz;
     if (total == 0) return;
     const u64 tiles = (total + BLOCK * IPT - 1) / (BLOCK * IPT);
-    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, tile_i0, core_idx, headp, dplus,
-                                                             spanning, ctl);
+    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning,
+                                                             ctl);
 }
 
 template <typename OffT>
