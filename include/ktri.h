@@ -119,6 +119,24 @@ int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint
 /* Synchronise the context's last stream and report device-side CSR errors of the last call. */
 int ktri_ctx_check(ktri_ctx* ctx);
 
+/* No counterpart in the reference: a count that allocates no memory.  For callers that
+ * cannot call cudaMalloc, such as a host runtime that owns all device memory through its
+ * own pool (where an allocation outside the pool breaks its accounting and can synchronise
+ * the device), or a latency-bound loop that must not pay for an allocation.  Same inputs and
+ * outputs as ktri_count_csr_device with the AUTO method (d_per_vertex is required here), and
+ * no context: the workspace is a fixed 64 MiB array in device memory, held by every GPU that
+ * loads this library until the process exits.  A graph fits when
+ * ktri_workspace_bytes(n, nnz, KTRI_METHOD_AUTO) <= 64 MiB (about 600 000 vertices with 16
+ * adjacency entries each); larger graphs return KTRI_ERR_UNSUPPORTED before anything is
+ * launched.
+ * The first call on a device looks up the array's device address (once per device, with
+ * that device current); make that first call before any stream capture.  All calls on a
+ * device share the one array and leave the last call's contents in it; calls whose work
+ * overlaps on the GPU race on it, so serialise them.  Runs on `stream` and returns when that
+ * work is done, with KTRI_ERR_INVALID_CSR for invalid input found on the device. */
+int ktri_count_csr_device_noalloc(const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t nnz,
+                                  uint64_t* d_total, uint64_t* d_per_vertex, void* stream);
+
 /* Oriented, id-sorted out-lists (the state of DistributedGraph after preprocessing,
  * shared_memory_cetric.h:72-103, restricted to out_adj, distributed_graph.h:512-514) as a
  * compact CSR: out_first_out[n+1] and out_head[nnz/2].  Host buffers; synchronous. */

@@ -87,6 +87,7 @@ SIGNATURES = {
     "ktri_count_csr_ctx": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts)]),
     "ktri_count_csr_device": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts), P]),
     "ktri_ctx_check": (ctypes.c_int, [P]),
+    "ktri_count_csr_device_noalloc": (ctypes.c_int, [P, P, U64, U64, P, P, P]),
     "ktri_orient_csr": (ctypes.c_int, [P, P, P, U64, U64, P, P]),
     "ktri_intersect_pairs": (ctypes.c_int, [P, I32, P, P, P, P, U64, P, P]),
     "ktri_graph_from_csr": (ctypes.c_int, [U64, P, P, PP]),

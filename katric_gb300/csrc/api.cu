@@ -289,6 +289,65 @@ int device_status(ktri_ctx* ctx) {
 std::mutex g_default_mu;
 std::map<int, ktri_ctx*> g_default;
 
+// ---- counting without allocation --------------------------------------------------------
+// Scratch of ktri_count_csr_device_noalloc: a fixed array in device memory that every GPU
+// which loads this library holds until the process exits.  All calls on a device share it.
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device with that device current.
+// In host code the array's name is only a host-side stand-in, never a device address.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+int noalloc_scratch(int device, void** out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return KTRI_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return KTRI_ERR_CUDA;
+        }
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return KTRI_OK;
+}
+
+// The AUTO pipeline (same kernels as ktri_count_csr_device) on a caller-free workspace.
+template <typename OffT>
+int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total, u64* cnt,
+                int sms, cudaStream_t st) {
+    auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
+    auto* deg = reinterpret_cast<u32*>(base + L.deg);
+    auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
+    void* vdesc = base + L.vdesc;
+    auto* headp = reinterpret_cast<u32*>(base + L.headp);
+    auto* spanning = reinterpret_cast<u32*>(base + L.spanning);
+    auto* partials = reinterpret_cast<u64*>(base + L.partials);
+    auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
+    auto* ltiles = reinterpret_cast<uint2*>(base + L.ltiles);
+    // the control block (counters, error word) must start at zero; k_prep zeroes the
+    // out-degrees and per-vertex counts; every other region is fully written before it is read
+    if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return KTRI_ERR_CUDA;
+    ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
+    ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, ltiles, (u32)ktri::SMALL_D, ktri::LARGE_SEG, ctl, sms, st);
+    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl, sms, st,
+                                      nullptr, nullptr) != cudaSuccess)
+        return KTRI_ERR_CUDA;
+    const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
+    ktri::launch_final(partials, np, d_total, ctl, st);
+    if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
+    u32 herr = 0;
+    if (cudaMemcpyAsync(&herr, &ctl->err, sizeof(u32), cudaMemcpyDeviceToHost, st) != cudaSuccess) return KTRI_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return KTRI_ERR_CUDA;
+    return (herr & ktri::DEV_ERR_MASK) ? KTRI_ERR_INVALID_CSR : KTRI_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -387,6 +446,40 @@ int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint
     auto* tot = reinterpret_cast<u64*>(d_total);
     if (L.wide) return run_pipeline<u64>(ctx, L, fo, d_head, n, nnz, tot, cnt, opt, st, false);
     return run_pipeline<u32>(ctx, L, fo, d_head, n, nnz, tot, cnt, opt, st, false);
+}
+
+int ktri_count_csr_device_noalloc(const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t nnz,
+                                  uint64_t* d_total, uint64_t* d_per_vertex, void* stream) {
+    if (!d_total || !d_per_vertex || (n && !d_first_out) || (nnz && !d_head)) return KTRI_ERR_INVALID_ARGUMENT;
+    if (n == 0 && nnz != 0) return KTRI_ERR_INVALID_CSR;
+    if (n > 0x7FFFFFFFull) return KTRI_ERR_UNSUPPORTED;
+    // the workspace must fit the fixed scratch array: checked before anything is launched
+    // (the same layout ktri_workspace_bytes reports; its per-vertex count region goes unused)
+    const Layout L = make_layout(n, nnz, KTRI_METHOD_AUTO, 0, false, true);
+    if (L.bytes > NOALLOC_SCRATCH_BYTES) return KTRI_ERR_UNSUPPORTED;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return KTRI_ERR_NO_DEVICE;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        if (cudaMemsetAsync(d_total, 0, sizeof(u64), st) != cudaSuccess) return KTRI_ERR_CUDA;
+        return cudaStreamSynchronize(st) == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
+    }
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(dev, &scratch);
+    if (rc) return rc;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return KTRI_ERR_CUDA;
+    if (sms > 160) return KTRI_ERR_UNSUPPORTED;  // the layout's partial-sum array is sized for 160 SMs
+    char* base = static_cast<char*>(scratch);
+    auto* fo = reinterpret_cast<const u64*>(d_first_out);
+    auto* tot = reinterpret_cast<u64*>(d_total);
+    auto* cnt = reinterpret_cast<u64*>(d_per_vertex);
+    if (L.wide) return run_noalloc<u64>(base, L, fo, d_head, n, nnz, tot, cnt, sms, st);
+    return run_noalloc<u32>(base, L, fo, d_head, n, nnz, tot, cnt, sms, st);
 }
 
 int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
