@@ -36,6 +36,10 @@ WORKLOADS = {
     "rmat20": dict(kind="rmat", scale=20, edge_factor=16, seed=2),
     "rmat22": dict(kind="rmat", scale=22, edge_factor=16, seed=2),
     "rgg20": dict(kind="rgg2d", n=1 << 20, avg_degree=32.0, seed=3),
+    # batched workload: many graphs, n log-uniform in [2^8, 2^17], degree U(4, 64),
+    # G(n,m) / RMAT / RGG by index mod 3, graph i seeded with 4 + i
+    "batch8192": dict(kind="batch", graphs=8192, log2_n=(8.0, 17.0), degree=(4.0, 64.0), seed=4),
+    "batch1024": dict(kind="batch", graphs=1024, log2_n=(8.0, 17.0), degree=(4.0, 64.0), seed=4),
 }
 METRIC = "edges/s (undirected edges / time of one exact total + per-vertex count)"
 KERNELS_PER_STEP = 6  # k_prep, k_orient, k_desc, k_count_small, k_count_large, k_final
@@ -178,6 +182,87 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Batched workload: one captured plan (CUDA graph) over the packed union of all graphs,
+    against the plain loop of one device entry-point call per graph, both timed here."""
+    import torch
+    from katric_gb300 import Batch, Config, TriangleCounter
+    w = WORKLOADS[args.workload]
+    t0 = time.perf_counter()
+    b = Batch.generate(w["graphs"], w["log2_n"][0], w["log2_n"][1], w["degree"][0], w["degree"][1], w["seed"])
+    gen_s = time.perf_counter() - t0
+    n, nnz, k = b.union.n, b.union.nnz, b.num_graphs
+    ctr = TriangleCounter(0)
+    dev = torch.device("cuda:0")
+    fo = torch.from_numpy(b.union.first_out.view(np.int64)).to(dev)
+    hd = torch.from_numpy(b.union.head.view(np.int32)).to(dev)
+    gf = torch.from_numpy(b.graph_first.view(np.int64)).to(dev)
+    tot = torch.zeros(k, dtype=torch.int64, device=dev)
+    pv = torch.zeros(n, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    plan = ctr.plan_batch(fo.data_ptr(), hd.data_ptr(), n, nnz, gf.data_ptr(), k, tot.data_ptr(), pv.data_ptr(),
+                          Config())
+    for _ in range(args.warmup):
+        plan.launch(stream.cuda_stream)
+    plan.check()
+    ref_tot = tot.clone()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        plan.launch(stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+    plan.check()
+    assert torch.equal(tot, ref_tot)
+    # plain loop: one ktri_count_csr_device call per graph on per-graph device CSRs
+    gfo = b.graph_first.astype(np.int64)
+    ufo = b.union.first_out.astype(np.int64)
+    per = []
+    for g in range(k):
+        a, e = gfo[g], gfo[g + 1]
+        f = fo[a:e + 1] - int(ufo[a])
+        h = (hd[int(ufo[a]):int(ufo[e])] - int(a)).to(torch.int32)
+        per.append((f.contiguous(), h.contiguous(), int(e - a), int(ufo[e] - ufo[a])))
+    out_t = torch.zeros(k, dtype=torch.int64, device=dev)
+    out_pv = torch.zeros(int(max(p[2] for p in per)) + 1, dtype=torch.int64, device=dev)
+    cfg = Config()
+
+    def plain_pass():
+        for g, (f, h, gn, gnnz) in enumerate(per):
+            ctr.count_device(f.data_ptr(), h.data_ptr(), gn, gnnz, out_t[g:g + 1].data_ptr(), out_pv.data_ptr(), cfg,
+                             stream=stream.cuda_stream)
+
+    plain_pass()  # warm-up (grows the workspace to the largest graph)
+    ctr.check()
+    assert torch.equal(out_t, ref_tot), "plain loop and batch disagree"
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    plain_pass()
+    ctr.check()
+    plain_ms = (time.perf_counter() - t1) * 1e3
+    line = {
+        "metric": METRIC + "; batched workload", "value": b.union.m / (ms / 1e3), "unit": "edges/s",
+        "graphs_per_s": k / (ms / 1e3), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded generators)",
+        "config": {"workload": args.workload, "graphs": k, "n_total": n, "m_total": b.union.m, "seed": w["seed"],
+                   "log2_n": list(w["log2_n"]), "degree": list(w["degree"]), "generation_s": round(gen_s, 2),
+                   "path": "one captured plan (CUDA graph) over the packed union"},
+        "plain_loop": {"ms": plain_ms, "graphs_per_s": k / (plain_ms / 1e3), "edges_per_s": b.union.m / (plain_ms / 1e3),
+                       "path": "ktri_count_csr_device per graph, one stream, device-resident inputs"},
+        "batched_vs_plain": plain_ms / ms,
+        "triangles_total": int(ref_tot.sum().item()),
+        "gpu_launches": 9 * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -192,6 +277,9 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if WORKLOADS[args.workload]["kind"] == "batch":
+        run_batch(args)
         return
 
     import torch

@@ -137,6 +137,33 @@ int ktri_ctx_check(ktri_ctx* ctx);
 int ktri_count_csr_device_noalloc(const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t nnz,
                                   uint64_t* d_total, uint64_t* d_per_vertex, void* stream);
 
+/* ---- batches of graphs ---------------------------------------------------------------------
+ * No counterpart in the reference (KaTric counts one graph per run).  Many independent graphs
+ * are packed as one disjoint-union CSR: graph g owns the vertices [graph_first[g],
+ * graph_first[g+1]) and its adjacency entries name only those vertices.  One launch sequence
+ * counts every graph (the merge-path and owner tiles of all graphs share one device work
+ * queue); totals[g] receives graph g's triangle count and per_vertex (optional) the union's
+ * per-vertex counts.  ktri_batch_pack / ktri_batch_generate build such a union on the host. */
+int ktri_count_batch_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                            uint64_t nnz_total, const uint64_t* d_graph_first, uint64_t num_graphs, uint64_t* d_totals,
+                            uint64_t* d_per_vertex, const ktri_opts* opts, void* stream);
+int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n_total,
+                         uint64_t nnz_total, const uint64_t* graph_first, uint64_t num_graphs, uint64_t* totals_out,
+                         uint64_t* per_vertex_out, const ktri_opts* opts);
+
+/* A captured plan: the launch sequence of one batch count recorded once as a CUDA graph and
+ * replayed by ktri_plan_launch (one graph launch instead of one launch per kernel).  The plan
+ * owns its workspace and is bound to the device buffers given here; refill those buffers with
+ * another batch of the same n_total / nnz_total / num_graphs and launch again.
+ * ktri_plan_check synchronises the last launch and reports invalid input found on the device. */
+typedef struct ktri_plan ktri_plan;
+int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                           uint64_t nnz_total, const uint64_t* d_graph_first, uint64_t num_graphs,
+                           uint64_t* d_totals, uint64_t* d_per_vertex, const ktri_opts* opts, ktri_plan** out);
+int ktri_plan_launch(ktri_plan* plan, void* stream);
+int ktri_plan_check(ktri_plan* plan);
+int ktri_plan_destroy(ktri_plan* plan);
+
 /* Oriented, id-sorted out-lists (the state of DistributedGraph after preprocessing,
  * shared_memory_cetric.h:72-103, restricted to out_adj, distributed_graph.h:512-514) as a
  * compact CSR: out_first_out[n+1] and out_head[nnz/2].  Host buffers; synchronous. */
@@ -160,7 +187,15 @@ int ktri_graph_from_csr(uint64_t n, const uint64_t* first_out, const uint32_t* h
 int ktri_graph_gnm(uint64_t n, uint64_t m, uint64_t seed, ktri_graph** out);
 int ktri_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
                     ktri_graph** out);
+int ktri_graph_rmat_n(uint64_t n, uint64_t samples, double a, double b, double c, uint64_t seed, ktri_graph** out);
 int ktri_graph_rgg2d(uint64_t n, double avg_degree, uint64_t seed, ktri_graph** out);
+/* Disjoint union of graphs (graph_first needs num_graphs + 1 entries). */
+int ktri_batch_pack(uint64_t num_graphs, const ktri_graph* const* graphs, ktri_graph** out, uint64_t* graph_first);
+/* The batched workload: num_graphs graphs with n = round(2^U(log2_n_min, log2_n_max)),
+ * average degree U(deg_min, deg_max), generator i mod 3 = G(n,m) / RMAT(0.57,0.19,0.19) / 2D
+ * RGG, graph i seeded with seed + i; returned packed as one union. */
+int ktri_batch_generate(uint64_t num_graphs, double log2_n_min, double log2_n_max, double deg_min, double deg_max,
+                        uint64_t seed, ktri_graph** out, uint64_t* graph_first);
 int ktri_graph_read_metis(const char* path, ktri_graph** out);
 int ktri_graph_read_binary(const char* stem, ktri_graph** out);
 int ktri_graph_write_binary(const ktri_graph* g, const char* stem);

@@ -5,11 +5,11 @@ per-vertex out-lists, set intersection, with a u64 total and u64 per-vertex coun
 The compute path is libktri.so (include/ktri.h); this package is its host mirror.
 """
 from ._native import KtriError, load
-from .counter import (Config, LocalStatistics, Statistics, TriangleCounter, default_counter, intersection,
+from .counter import (Config, LocalStatistics, Plan, Statistics, TriangleCounter, default_counter, intersection,
                       preprocessing, run_shmem)
-from .graph import Graph, generate
+from .graph import Batch, Graph, generate
 
 __all__ = [
-    "Config", "Graph", "KtriError", "LocalStatistics", "Statistics", "TriangleCounter", "default_counter",
+    "Batch", "Config", "Graph", "Plan", "KtriError", "LocalStatistics", "Statistics", "TriangleCounter", "default_counter",
     "generate", "intersection", "load", "preprocessing", "run_shmem",
 ]

@@ -88,12 +88,21 @@ SIGNATURES = {
     "ktri_count_csr_device": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts), P]),
     "ktri_ctx_check": (ctypes.c_int, [P]),
     "ktri_count_csr_device_noalloc": (ctypes.c_int, [P, P, U64, U64, P, P, P]),
+    "ktri_count_batch_device": (ctypes.c_int, [P, P, P, U64, U64, P, U64, P, P, ctypes.POINTER(Opts), P]),
+    "ktri_count_batch_ctx": (ctypes.c_int, [P, P, P, U64, U64, P, U64, P, P, ctypes.POINTER(Opts)]),
+    "ktri_plan_create_batch": (ctypes.c_int, [P, P, P, U64, U64, P, U64, P, P, ctypes.POINTER(Opts), PP]),
+    "ktri_plan_launch": (ctypes.c_int, [P, P]),
+    "ktri_plan_check": (ctypes.c_int, [P]),
+    "ktri_plan_destroy": (ctypes.c_int, [P]),
     "ktri_orient_csr": (ctypes.c_int, [P, P, P, U64, U64, P, P]),
     "ktri_intersect_pairs": (ctypes.c_int, [P, I32, P, P, P, P, U64, P, P]),
     "ktri_graph_from_csr": (ctypes.c_int, [U64, P, P, PP]),
     "ktri_graph_gnm": (ctypes.c_int, [U64, U64, U64, PP]),
     "ktri_graph_rmat": (ctypes.c_int, [U32, U32, D, D, D, U64, PP]),
+    "ktri_graph_rmat_n": (ctypes.c_int, [U64, U64, D, D, D, U64, PP]),
     "ktri_graph_rgg2d": (ctypes.c_int, [U64, D, U64, PP]),
+    "ktri_batch_pack": (ctypes.c_int, [U64, P, PP, P]),
+    "ktri_batch_generate": (ctypes.c_int, [U64, D, D, D, D, U64, PP, P]),
     "ktri_graph_read_metis": (ctypes.c_int, [CP, PP]),
     "ktri_graph_read_binary": (ctypes.c_int, [CP, PP]),
     "ktri_graph_write_binary": (ctypes.c_int, [P, CP]),

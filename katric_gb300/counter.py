@@ -19,7 +19,7 @@ from typing import Optional
 import numpy as np
 
 from . import _native
-from .graph import Graph
+from .graph import Batch, Graph
 
 METHOD_BY_NAME = {
     "auto": _native.METHOD_AUTO,
@@ -159,6 +159,40 @@ class TriangleCounter:
         self._check(self._L.ktri_ctx_stats(self._ctx, ctypes.byref(st)))
         return st
 
+    def count_batch(self, batch: Batch, conf: Config | None = None, per_vertex: bool = True):
+        """Host batch in, (per-graph totals, union per-vertex counts or None) out; one launch sequence."""
+        conf = conf or Config()
+        fo, hd, gf = batch.union.first_out, batch.union.head, batch.graph_first
+        n, nnz, k = batch.union.n, batch.union.nnz, batch.num_graphs
+        totals = np.zeros(max(1, k), dtype=np.uint64)
+        pv = np.zeros(max(1, n), dtype=np.uint64) if per_vertex else None
+        opts = conf.opts()
+        self._check(self._L.ktri_count_batch_ctx(self._ctx, fo.ctypes.data, hd.ctypes.data if nnz else None, n, nnz,
+                                                 gf.ctypes.data, k, totals.ctypes.data,
+                                                 pv.ctypes.data if pv is not None else None, ctypes.byref(opts)))
+        return totals[:k], (pv[:n] if pv is not None else None)
+
+    def count_batch_device(self, first_out_ptr: int, head_ptr: int, n_total: int, nnz_total: int,
+                           graph_first_ptr: int, num_graphs: int, totals_ptr: int, per_vertex_ptr: int | None = None,
+                           conf: Config | None = None, stream: int = 0) -> None:
+        conf = conf or Config()
+        opts = conf.opts()
+        self._check(self._L.ktri_count_batch_device(self._ctx, first_out_ptr, head_ptr, n_total, nnz_total,
+                                                    graph_first_ptr, num_graphs, totals_ptr, per_vertex_ptr,
+                                                    ctypes.byref(opts), stream or None))
+
+    def plan_batch(self, first_out_ptr: int, head_ptr: int, n_total: int, nnz_total: int, graph_first_ptr: int,
+                   num_graphs: int, totals_ptr: int, per_vertex_ptr: int | None = None,
+                   conf: Config | None = None) -> "Plan":
+        """Capture one batch count as a CUDA graph bound to these device buffers."""
+        conf = conf or Config()
+        opts = conf.opts()
+        h = ctypes.c_void_p()
+        self._check(self._L.ktri_plan_create_batch(self._ctx, first_out_ptr, head_ptr, n_total, nnz_total,
+                                                   graph_first_ptr, num_graphs, totals_ptr, per_vertex_ptr,
+                                                   ctypes.byref(opts), ctypes.byref(h)))
+        return Plan(self, h)
+
     def orient(self, first_out, head):
         """Oriented, id-sorted out-lists as a compact CSR (u64 offsets, u32 ids)."""
         fo = np.ascontiguousarray(first_out, dtype=np.uint64)
@@ -190,6 +224,31 @@ class TriangleCounter:
         if not members:
             return [int(c) for c in counts[: len(pairs)]]
         return [[int(x) for x in mem[int(a_off[i]): int(a_off[i]) + int(counts[i])]] for i in range(len(pairs))]
+
+
+class Plan:
+    """A captured batch count (CUDA graph); launch() replays it on a stream."""
+
+    def __init__(self, counter: TriangleCounter, handle):
+        self._counter = counter
+        self._h = handle
+
+    def launch(self, stream: int = 0) -> None:
+        self._counter._check(self._counter._L.ktri_plan_launch(self._h, stream or None))
+
+    def check(self) -> None:
+        self._counter._check(self._counter._L.ktri_plan_check(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self._counter._L.ktri_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default: dict[int, TriangleCounter] = {}

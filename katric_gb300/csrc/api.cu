@@ -175,9 +175,8 @@ struct DeviceGuard {
 };
 
 template <typename OffT>
-int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total,
-                 u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all) {
-    char* base = static_cast<char*>(ctx->ws);
+int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz,
+                     u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all, bool events) {
     auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
     auto* deg = reinterpret_cast<u32*>(base + L.deg);
     auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
@@ -189,7 +188,7 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
     const int sms = ctx->num_sms;
 
     KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
-    KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
+    if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
     const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
@@ -201,14 +200,15 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
                                       L.scratch_per_block, L.big_grid, ctl, sms, st);
     }
-    KTRI_CK(ctx, cudaEventRecord(ctx->ev[1], st));
+    if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[1], st));
     if (opt.collect_stats) ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, ctl, sms, st);
-    KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
+    if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl, sms, st,
-                                                   ctx->ev[4], ctx->ev[5]));
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl,
+                                                   sms, st, events ? ctx->ev[4] : nullptr,
+                                                   events ? ctx->ev[5] : nullptr));
         const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
         ktri::launch_final(partials, np, d_total, ctl, st);
     } else {
@@ -217,9 +217,19 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
                                        grid, ctl, st);
         ktri::launch_final(partials, (u32)grid, d_total, ctl, st);
     }
-    KTRI_CK(ctx, cudaEventRecord(ctx->ev[3], st));
+    if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[3], st));
     KTRI_CK(ctx, cudaGetLastError());
-    ctx->ctl = ctl;
+    return KTRI_OK;
+}
+
+// Enqueue a count on the context's workspace and remember it for ktri_ctx_check / stats.
+template <typename OffT>
+int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total,
+                 u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all) {
+    char* base = static_cast<char*>(ctx->ws);
+    const int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, sort_all, true);
+    if (rc) return rc;
+    ctx->ctl = reinterpret_cast<Control*>(base + L.ctl);
     ctx->last_stream = st;
     ctx->pending = true;
     ctx->have_events = true;
@@ -534,6 +544,244 @@ int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, 
         }
     }
     return ktri_count_csr_ctx(ctx, first_out, head, n, nnz, total_out, per_vertex_out, opts);
+}
+
+// ---- batches of graphs ----------------------------------------------------------------
+
+}  // extern "C"
+
+namespace {
+
+int check_batch(ktri_ctx* ctx, const void* fo, const void* head, u64 n, u64 nnz, const void* graph_first,
+                u64 num_graphs, const void* totals, const ktri::Options& opt) {
+    int rc = check_common(ctx, fo, head, n, nnz, totals, opt);
+    if (rc) return rc;
+    if (num_graphs && !graph_first) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "graph_first is NULL");
+    return KTRI_OK;
+}
+
+template <typename OffT>
+int enqueue_batch(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz,
+                  const u64* graph_first, u64 num_graphs, u64* totals, u64* cnt, const ktri::Options& opt,
+                  cudaStream_t st, bool events) {
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, false, events);
+    if (rc) return rc;
+    ktri::launch_graph_totals(cnt, graph_first, num_graphs, n, totals, reinterpret_cast<Control*>(base + L.ctl),
+                              ctx->num_sms, st);
+    KTRI_CK(ctx, cudaGetLastError());
+    return KTRI_OK;
+}
+
+void note_pending(ktri_ctx* ctx, const Layout& L, char* base, cudaStream_t st, u64 n, u64 nnz,
+                  const ktri::Options& opt) {
+    ctx->ctl = reinterpret_cast<Control*>(base + L.ctl);
+    ctx->last_stream = st;
+    ctx->pending = true;
+    ctx->have_events = true;
+    ctx->last_method = opt.method;
+    ctx->last_collect = opt.collect_stats;
+    ctx->stats = ktri_run_stats{};
+    ctx->stats.n = n;
+    ctx->stats.nnz = nnz;
+    ctx->stats.method = (u32)opt.method;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ktri_count_batch_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                            uint64_t nnz_total, const uint64_t* d_graph_first, uint64_t num_graphs, uint64_t* d_totals,
+                            uint64_t* d_per_vertex, const ktri_opts* opts, void* stream) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_batch(ctx, d_first_out, d_head, n_total, nnz_total, d_graph_first, num_graphs, d_totals, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n_total == 0) {
+        if (num_graphs) KTRI_CK(ctx, cudaMemsetAsync(d_totals, 0, sizeof(u64) * num_graphs, st));
+        ctx->pending = false;
+        return KTRI_OK;
+    }
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex) : reinterpret_cast<u64*>(base + L.cnt);
+    auto* fo = reinterpret_cast<const u64*>(d_first_out);
+    auto* gf = reinterpret_cast<const u64*>(d_graph_first);
+    auto* tot = reinterpret_cast<u64*>(d_totals);
+    rc = L.wide ? enqueue_batch<u64>(ctx, base, L, fo, d_head, n_total, nnz_total, gf, num_graphs, tot, cnt, opt, st,
+                                     true)
+                : enqueue_batch<u32>(ctx, base, L, fo, d_head, n_total, nnz_total, gf, num_graphs, tot, cnt, opt, st,
+                                     true);
+    if (rc) return rc;
+    note_pending(ctx, L, base, st, n_total, nnz_total, opt);
+    return KTRI_OK;
+}
+
+int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n_total,
+                         uint64_t nnz_total, const uint64_t* graph_first, uint64_t num_graphs, uint64_t* totals_out,
+                         uint64_t* per_vertex_out, const ktri_opts* opts) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_batch(ctx, first_out, head, n_total, nnz_total, graph_first, num_graphs, totals_out, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    for (u64 i = 0; i < num_graphs; ++i)
+        if (graph_first[i + 1] < graph_first[i] || graph_first[i + 1] > n_total)
+            return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "graph_first must be non-decreasing and end within n");
+    if (num_graphs && (graph_first[0] != 0 || graph_first[num_graphs] != n_total))
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "graph_first must run from 0 to n_total");
+    if (n_total == 0) {
+        for (u64 i = 0; i < num_graphs; ++i) totals_out[i] = 0;
+        return KTRI_OK;
+    }
+    if (first_out[0] != 0 || first_out[n_total] != nnz_total)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, true, true);
+    const size_t off_gf = L.bytes, off_tot = align_up(off_gf + sizeof(u64) * (num_graphs + 1));
+    const size_t total_bytes = align_up(off_tot + sizeof(u64) * (num_graphs + 1));
+    rc = ensure_ws(ctx, total_bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_gf = reinterpret_cast<u64*>(base + off_gf);
+    auto* d_tot = reinterpret_cast<u64*>(base + off_tot);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n_total + 1), cudaMemcpyHostToDevice, st));
+    if (nnz_total) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz_total, cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(d_gf, graph_first, sizeof(u64) * (num_graphs + 1), cudaMemcpyHostToDevice, st));
+    rc = L.wide ? enqueue_batch<u64>(ctx, base, L, d_fo, d_head, n_total, nnz_total, d_gf, num_graphs, d_tot, d_cnt,
+                                     opt, st, true)
+                : enqueue_batch<u32>(ctx, base, L, d_fo, d_head, n_total, nnz_total, d_gf, num_graphs, d_tot, d_cnt,
+                                     opt, st, true);
+    if (rc) return rc;
+    note_pending(ctx, L, base, st, n_total, nnz_total, opt);
+    if (num_graphs) KTRI_CK(ctx, cudaMemcpyAsync(totals_out, d_tot, sizeof(u64) * num_graphs, cudaMemcpyDeviceToHost, st));
+    if (per_vertex_out)
+        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n_total, cudaMemcpyDeviceToHost, st));
+    return device_status(ctx);
+}
+
+// ---- captured plans ----------------------------------------------------------------------
+
+}  // extern "C"
+
+struct ktri_plan {
+    ktri_ctx* ctx = nullptr;
+    void* ws = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Control* ctl = nullptr;
+    cudaStream_t last = nullptr;
+    bool launched = false;
+};
+
+extern "C" {
+
+int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                           uint64_t nnz_total, const uint64_t* d_graph_first, uint64_t num_graphs,
+                           uint64_t* d_totals, uint64_t* d_per_vertex, const ktri_opts* opts, ktri_plan** out) {
+    if (!out) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    const ktri::Options opt = resolve(opts);
+    int rc = check_batch(ctx, d_first_out, d_head, n_total, nnz_total, d_graph_first, num_graphs, d_totals, opt);
+    if (rc) return rc;
+    if (n_total == 0) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "a plan needs at least one vertex");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true);
+    if (ctx->budget && L.bytes > ctx->budget)
+        return set_error(ctx, KTRI_ERR_OUT_OF_MEMORY, "plan workspace exceeds the memory budget");
+    ktri_plan* p = new (std::nothrow) ktri_plan();
+    if (!p) return KTRI_ERR_OUT_OF_MEMORY;
+    p->ctx = ctx;
+    cudaError_t e = cudaMalloc(&p->ws, L.bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete p;
+        return cuda_fail(ctx, e, "cudaMalloc(plan workspace)");
+    }
+    // occupancy queries happen once, outside the capture
+    (void)ktri::count_grid_small<u32>(ctx->num_sms);
+    (void)ktri::count_grid_large<u32>(ctx->num_sms);
+    (void)ktri::count_grid_small<u64>(ctx->num_sms);
+    (void)ktri::count_grid_large<u64>(ctx->num_sms);
+    cudaStream_t cs = nullptr;
+    cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    char* base = static_cast<char*>(p->ws);
+    u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex) : reinterpret_cast<u64*>(base + L.cnt);
+    auto* fo = reinterpret_cast<const u64*>(d_first_out);
+    auto* gf = reinterpret_cast<const u64*>(d_graph_first);
+    auto* tot = reinterpret_cast<u64*>(d_totals);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        rc = L.wide ? enqueue_batch<u64>(ctx, base, L, fo, d_head, n_total, nnz_total, gf, num_graphs, tot, cnt, opt, cs,
+                                         false)
+                    : enqueue_batch<u32>(ctx, base, L, fo, d_head, n_total, nnz_total, gf, num_graphs, tot, cnt, opt, cs,
+                                         false);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (rc == KTRI_OK && e2 != cudaSuccess) rc = cuda_fail(ctx, e2, "cudaStreamEndCapture");
+        p->graph = graph;
+        if (rc == KTRI_OK) {
+            const cudaError_t e3 = cudaGraphInstantiate(&p->exec, graph, 0);
+            if (e3 != cudaSuccess) rc = cuda_fail(ctx, e3, "cudaGraphInstantiate");
+        }
+    } else {
+        rc = cuda_fail(ctx, e, "cudaStreamBeginCapture");
+    }
+    cudaStreamDestroy(cs);
+    if (rc) {
+        if (p->exec) cudaGraphExecDestroy(p->exec);
+        if (p->graph) cudaGraphDestroy(p->graph);
+        cudaFree(p->ws);
+        delete p;
+        return rc;
+    }
+    p->ctl = reinterpret_cast<Control*>(base + L.ctl);
+    *out = p;
+    return KTRI_OK;
+}
+
+int ktri_plan_launch(ktri_plan* plan, void* stream) {
+    if (!plan) return KTRI_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(plan->ctx->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    KTRI_CK(plan->ctx, cudaGraphLaunch(plan->exec, st));
+    plan->last = st;
+    plan->launched = true;
+    return KTRI_OK;
+}
+
+int ktri_plan_check(ktri_plan* plan) {
+    if (!plan) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!plan->launched) return KTRI_OK;
+    DeviceGuard g(plan->ctx->device);
+    ktri_ctx* ctx = plan->ctx;
+    KTRI_CK(ctx, cudaStreamSynchronize(plan->last));
+    u32 err = 0;
+    KTRI_CK(ctx, cudaMemcpy(&err, &plan->ctl->err, sizeof(u32), cudaMemcpyDeviceToHost));
+    if (err & ktri::DEV_ERR_MASK) return set_error(ctx, KTRI_ERR_INVALID_CSR, "invalid CSR found on the device");
+    return KTRI_OK;
+}
+
+int ktri_plan_destroy(ktri_plan* plan) {
+    if (!plan) return KTRI_ERR_INVALID_ARGUMENT;
+    {
+        DeviceGuard g(plan->ctx->device);
+        if (plan->launched) cudaStreamSynchronize(plan->last);
+        if (plan->exec) cudaGraphExecDestroy(plan->exec);
+        if (plan->graph) cudaGraphDestroy(plan->graph);
+        if (plan->ws) cudaFree(plan->ws);
+    }
+    delete plan;
+    return KTRI_OK;
 }
 
 int ktri_orient_csr(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,

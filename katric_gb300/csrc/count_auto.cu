@@ -483,6 +483,27 @@ __global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials
     if (threadIdx.x == 0) *total = t;
 }
 
+// Batched counting: per-graph totals of a disjoint union (graph g owns the vertices
+// [graph_first[g], graph_first[g+1])).  Every triangle adds one to each of its three corners,
+// all inside one graph, so a graph's total is the sum of its per-vertex counts over three.
+__global__ void __launch_bounds__(256) k_graph_totals(const u64* __restrict__ cnt, const u64* __restrict__ graph_first,
+                                                      u64 num_graphs, u64 n, u64* __restrict__ totals, Control* ctl) {
+    __shared__ u64 s_red[8];
+    if (ctl->err & DEV_ERR_MASK) return;
+    for (u64 g = blockIdx.x; g < num_graphs; g += gridDim.x) {
+        const u64 a = graph_first[g], b = graph_first[g + 1];
+        const bool ok = a <= b && b <= n;
+        u64 s = 0;
+        if (ok)
+            for (u64 v = a + threadIdx.x; v < b; v += 256) s += cnt[v];
+        s = block_sum_u64<256>(s, s_red);
+        if (threadIdx.x == 0) {
+            totals[g] = ok ? s / 3 : 0;
+            if (!ok) atomicOr(&ctl->err, DEV_ERR_DEGREE);
+        }
+    }
+}
+
 // collect_stats: wedge_checks = sum over oriented (v,u) of |N+(u)|, the reference's counter
 // (cetric_edge_iterator.h:279-281), plus the entries streamed by the AUTO kernels.
 template <typename OffT>
@@ -581,6 +602,13 @@ cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, co
         <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs, ctl);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
+}
+
+void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs, u64 n, u64* totals, Control* ctl,
+                         int num_sms, cudaStream_t st) {
+    if (num_graphs == 0) return;
+    u64 blocks = num_graphs < (u64)num_sms * 8 ? num_graphs : (u64)num_sms * 8;
+    k_graph_totals<<<(unsigned)blocks, 256, 0, st>>>(cnt, graph_first, num_graphs, n, totals, ctl);
 }
 
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st) {

@@ -181,23 +181,23 @@ int ktri_graph_gnm(uint64_t n, uint64_t m, uint64_t seed, ktri_graph** out) {
     return KTRI_OK;
 }
 
-// RMAT: 2^scale vertices, edge_factor * 2^scale samples; each sample descends `scale`
-// levels choosing quadrant a (0,0), b (0,1), c (1,0) or d (1,1).  Symmetrised,
-// deduplicated, self-loops removed, no vertex permutation.
-int ktri_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
-                    ktri_graph** out) {
+// RMAT on n vertices: each of `samples` draws descends ceil(log2 n) levels choosing quadrant
+// a (0,0), b (0,1), c (1,0) or d (1,1); draws that land outside [0, n)^2 are dropped.
+// Symmetrised, deduplicated, self-loops removed, no vertex permutation.  For n = 2^scale this
+// is the classic generator (nothing is dropped).
+int ktri_graph_rmat_n(uint64_t n, uint64_t samples, double a, double b, double c, uint64_t seed, ktri_graph** out) {
     if (!out) return KTRI_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    if (scale < 1 || scale > 31 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return KTRI_ERR_INVALID_ARGUMENT;
-    const uint64_t n = 1ull << scale;
-    const uint64_t samples = (uint64_t)edge_factor << scale;
+    if (n < 2 || n > (1ull << 31) || a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return KTRI_ERR_INVALID_ARGUMENT;
+    uint32_t scale = 0;
+    while ((1ull << scale) < n) ++scale;
     // 32-bit thresholds on a uniform 32-bit draw per level
     const double two32 = 4294967296.0;
     const uint64_t ta = (uint64_t)std::floor(a * two32);
     const uint64_t tb = (uint64_t)std::floor((a + b) * two32);
     const uint64_t tc = (uint64_t)std::floor((a + b + c) * two32);
     auto produce = [&](uint64_t i, uint32_t* u, uint32_t* v) {
-        uint32_t x = 0, y = 0;
+        uint64_t x = 0, y = 0;
         uint64_t r = 0;
         for (uint32_t lvl = 0; lvl < scale; ++lvl) {
             if ((lvl & 1u) == 0) r = rng_at(seed, 2, i * 16 + lvl / 2);
@@ -210,14 +210,24 @@ int ktri_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, do
             x = (x << 1) | bx;
             y = (y << 1) | by;
         }
-        *u = x;
-        *v = y;
+        if (x >= n || y >= n) return false;
+        *u = (uint32_t)x;
+        *v = (uint32_t)y;
         return true;
     };
     ktri_graph* g = build_from_samples(n, samples, produce);
     if (!g) return KTRI_ERR_OUT_OF_MEMORY;
     *out = g;
     return KTRI_OK;
+}
+
+// RMAT: 2^scale vertices, edge_factor * 2^scale samples.
+int ktri_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                    ktri_graph** out) {
+    if (!out) return KTRI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (scale < 1 || scale > 31) return KTRI_ERR_INVALID_ARGUMENT;
+    return ktri_graph_rmat_n(1ull << scale, (uint64_t)edge_factor << scale, a, b, c, seed, out);
 }
 
 // 2D random geometric graph: n points uniform in [0,1)^2, edge iff squared distance < r^2,
@@ -428,6 +438,80 @@ int ktri_graph_write_metis(const ktri_graph* g, const char* path) {
     }
     bool ok = std::fclose(f) == 0;
     return ok ? KTRI_OK : KTRI_ERR_IO;
+}
+
+// Disjoint union of graphs: graph k's vertices become [graph_first[k], graph_first[k+1]).
+static ktri_graph* pack_union(const std::vector<ktri_graph*>& gs, uint64_t* graph_first) {
+    const size_t k = gs.size();
+    std::vector<uint64_t> nnz_first(k + 1, 0);
+    graph_first[0] = 0;
+    for (size_t i = 0; i < k; ++i) {
+        graph_first[i + 1] = graph_first[i] + gs[i]->n;
+        nnz_first[i + 1] = nnz_first[i] + gs[i]->head.size();
+    }
+    if (graph_first[k] > 0xFFFFFFFFull) return nullptr;
+    ktri_graph* u = new_graph(graph_first[k], nnz_first[k]);
+    if (!u) return nullptr;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t ii = 0; ii < (int64_t)k; ++ii) {
+        const ktri_graph* g = gs[(size_t)ii];
+        const uint64_t vb = graph_first[ii], eb = nnz_first[ii];
+        for (uint64_t v = 0; v < g->n; ++v) u->first_out[vb + v + 1] = eb + g->first_out[v + 1];
+        for (uint64_t e = 0; e < g->head.size(); ++e) u->head[eb + e] = (uint32_t)(g->head[e] + vb);
+    }
+    return u;
+}
+
+int ktri_batch_pack(uint64_t num_graphs, const ktri_graph* const* graphs, ktri_graph** out, uint64_t* graph_first) {
+    if (!out || !graph_first || (num_graphs && !graphs)) return KTRI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::vector<ktri_graph*> gs(num_graphs);
+    for (uint64_t i = 0; i < num_graphs; ++i) {
+        if (!graphs[i]) return KTRI_ERR_INVALID_ARGUMENT;
+        gs[i] = const_cast<ktri_graph*>(graphs[i]);
+    }
+    ktri_graph* u = pack_union(gs, graph_first);
+    if (!u) return graph_first[num_graphs] > 0xFFFFFFFFull ? KTRI_ERR_UNSUPPORTED : KTRI_ERR_OUT_OF_MEMORY;
+    *out = u;
+    return KTRI_OK;
+}
+
+// A batch of independent graphs: graph i has n_i = round(2^U(log2_n_min, log2_n_max))
+// vertices and average degree d_i = U(deg_min, deg_max); generator i mod 3 picks G(n,m)
+// (m = round(n d / 2)), RMAT (0.57, 0.19, 0.19, 0.05) with round(n d / 2) draws, or the 2D
+// RGG; graph i is seeded with seed + i.  Graphs are generated in parallel, one per thread.
+int ktri_batch_generate(uint64_t num_graphs, double log2_n_min, double log2_n_max, double deg_min, double deg_max,
+                        uint64_t seed, ktri_graph** out, uint64_t* graph_first) {
+    if (!out || !graph_first) return KTRI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!(log2_n_min >= 1) || log2_n_max < log2_n_min || log2_n_max > 31 || !(deg_min >= 0) || deg_max < deg_min)
+        return KTRI_ERR_INVALID_ARGUMENT;
+    std::vector<ktri_graph*> gs(num_graphs, nullptr);
+    std::atomic<int> rc{KTRI_OK};
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t ii = 0; ii < (int64_t)num_graphs; ++ii) {
+        const uint64_t i = (uint64_t)ii;
+        const double u1 = unit_double(rng_at(seed, 4, 2 * i)), u2 = unit_double(rng_at(seed, 4, 2 * i + 1));
+        uint64_t n = (uint64_t)std::llround(std::exp2(log2_n_min + (log2_n_max - log2_n_min) * u1));
+        if (n < 2) n = 2;
+        const double d = deg_min + (deg_max - deg_min) * u2;
+        const uint64_t half = (uint64_t)std::llround((double)n * d / 2.0);
+        int r;
+        switch (i % 3) {
+            case 0: r = ktri_graph_gnm(n, std::min(half, n * (n - 1) / 2), seed + i, &gs[i]); break;
+            case 1: r = ktri_graph_rmat_n(n, half, 0.57, 0.19, 0.19, seed + i, &gs[i]); break;
+            default: r = ktri_graph_rgg2d(n, d, seed + i, &gs[i]); break;
+        }
+        if (r != KTRI_OK) rc.store(r);
+    }
+    int result = rc.load();
+    if (result == KTRI_OK) {
+        ktri_graph* u = pack_union(gs, graph_first);
+        if (!u) result = graph_first[num_graphs] > 0xFFFFFFFFull ? KTRI_ERR_UNSUPPORTED : KTRI_ERR_OUT_OF_MEMORY;
+        else *out = u;
+    }
+    for (ktri_graph* g : gs) delete g;
+    return result;
 }
 
 uint64_t ktri_graph_n(const ktri_graph* g) { return g ? g->n : 0; }

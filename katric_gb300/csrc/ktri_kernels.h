@@ -54,6 +54,8 @@ cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, co
                               int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
+void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs, u64 n, u64* totals, Control* ctl,
+                         int num_sms, cudaStream_t st);
 
 // Work counters of the reference (wedge_checks, intersection_size_local) and of the AUTO
 // kernels, accumulated into the control block.

@@ -13,13 +13,36 @@ import numpy as np
 from . import _native
 
 
+class _NativeGraph:
+    """Owns one ktri_graph; every numpy view of its arrays holds a reference to it."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def __del__(self):
+        if self.handle is not None:
+            try:
+                _native.load(build_if_missing=False).ktri_graph_free(self.handle)
+            except Exception:
+                pass
+            self.handle = None
+
+
+def _view(owner: _NativeGraph, ptr: int, ctype, count: int, dtype) -> np.ndarray:
+    if count == 0:
+        return np.zeros(0, dtype=dtype)
+    buf = (ctype * count).from_address(ptr)
+    buf._owner = owner  # the array's base keeps the native graph alive
+    return np.ctypeslib.as_array(buf)
+
+
 class Graph:
     """CSR graph on the host.  first_out: u64[n+1], head: u32[nnz]."""
 
-    def __init__(self, first_out, head, *, _handle=None):
+    def __init__(self, first_out, head, *, _owner=None):
         self.first_out = np.ascontiguousarray(first_out, dtype=np.uint64)
         self.head = np.ascontiguousarray(head, dtype=np.uint32)
-        self._handle = _handle  # keeps native memory alive when the arrays are views of it
+        self._owner = _owner  # native graph behind the arrays, if they are views of one
         if len(self.first_out) == 0:
             raise ValueError("first_out needs n+1 entries")
 
@@ -44,26 +67,16 @@ class Graph:
         d = self.degree().astype(np.uint64)
         return int(np.sum(d * (d - 1) // 2, dtype=np.uint64)) if len(d) else 0
 
-    def __del__(self):
-        h = getattr(self, "_handle", None)
-        if h is not None:
-            try:
-                _native.load(build_if_missing=False).ktri_graph_free(h)
-            except Exception:
-                pass
-            self._handle = None
-
     # ---- construction -------------------------------------------------------------------
     @staticmethod
     def _from_handle(h) -> "Graph":
         L = _native.load()
+        owner = _NativeGraph(h)
         n = L.ktri_graph_n(h)
         nnz = L.ktri_graph_nnz(h)
-        fo_ptr = L.ktri_graph_first_out(h)
-        hd_ptr = L.ktri_graph_head(h)
-        fo = np.ctypeslib.as_array((ctypes.c_uint64 * (n + 1)).from_address(fo_ptr)) if n + 1 else np.zeros(1, np.uint64)
-        hd = np.ctypeslib.as_array((ctypes.c_uint32 * nnz).from_address(hd_ptr)) if nnz else np.zeros(0, np.uint32)
-        return Graph(fo, hd, _handle=h)
+        fo = _view(owner, L.ktri_graph_first_out(h), ctypes.c_uint64, n + 1, np.uint64)
+        hd = _view(owner, L.ktri_graph_head(h), ctypes.c_uint32, nnz, np.uint32)
+        return Graph(fo, hd, _owner=owner)
 
     @staticmethod
     def _call(fn, *args) -> "Graph":
@@ -107,13 +120,14 @@ class Graph:
         raise ValueError(f"unknown input format {input_format!r} (metis or binary)")
 
     def _native_handle(self):
-        if self._handle is not None:
-            return self._handle
+        """A native graph with this graph's content (the backing one, or a copy)."""
+        if self._owner is not None:
+            return self._owner.handle
         h = ctypes.c_void_p()
         L = _native.load()
         _native.check(L.ktri_graph_from_csr(self.n, self.first_out.ctypes.data,
                                             self.head.ctypes.data if self.nnz else None, ctypes.byref(h)))
-        self._handle = h
+        self._owner = _NativeGraph(h)
         return h
 
     def write_binary(self, stem: str) -> None:
@@ -134,3 +148,46 @@ def generate(name: str, seed: int | None = None, **kw) -> Graph:
     if name in ("rgg2d", "rgg_2d"):
         return Graph.rgg2d(kw["n"], kw.get("avg_degree", 32.0), 3 if seed is None else seed)
     raise ValueError(f"unknown generator {name!r}")
+
+
+class Batch:
+    """Independent graphs packed as one disjoint-union CSR.
+
+    Graph g owns the union's vertices [graph_first[g], graph_first[g+1]); the union is what
+    the batched entry points count in one launch sequence."""
+
+    def __init__(self, union: Graph, graph_first):
+        self.union = union
+        self.graph_first = np.ascontiguousarray(graph_first, dtype=np.uint64)
+
+    @property
+    def num_graphs(self) -> int:
+        return len(self.graph_first) - 1
+
+    def graph(self, g: int) -> Graph:
+        """Graph g with its own 0-based ids."""
+        a, b = int(self.graph_first[g]), int(self.graph_first[g + 1])
+        fo = self.union.first_out[a:b + 1]
+        hd = self.union.head[int(fo[0]):int(fo[-1])]
+        return Graph(fo - fo[0], (hd.astype(np.int64) - a).astype(np.uint32))
+
+    @classmethod
+    def pack(cls, graphs) -> "Batch":
+        L = _native.load()
+        handles = (ctypes.c_void_p * max(1, len(graphs)))(*[g._native_handle() for g in graphs])
+        gf = np.zeros(len(graphs) + 1, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        _native.check(L.ktri_batch_pack(len(graphs), handles, ctypes.byref(h), gf.ctypes.data))
+        return cls(Graph._from_handle(h), gf)
+
+    @classmethod
+    def generate(cls, num_graphs: int = 8192, log2_n_min: float = 8.0, log2_n_max: float = 17.0,
+                 deg_min: float = 4.0, deg_max: float = 64.0, seed: int = 4) -> "Batch":
+        """The batched workload: n log-uniform, average degree uniform, generators G(n,m) / RMAT /
+        2D RGG by index mod 3, graph i seeded with seed + i."""
+        L = _native.load()
+        gf = np.zeros(num_graphs + 1, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        _native.check(L.ktri_batch_generate(num_graphs, log2_n_min, log2_n_max, deg_min, deg_max, seed,
+                                            ctypes.byref(h), gf.ctypes.data))
+        return cls(Graph._from_handle(h), gf)
