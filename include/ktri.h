@@ -54,7 +54,9 @@ typedef struct ktri_opts {
     uint32_t collect_stats;        /* 1: also compute wedge_checks / intersection work counters */
     uint64_t binary_intersection_cutoff; /* Config::binary_intersection_cutoff (config.h:173), default 1000 */
     double hybrid_cutoff_scale;    /* Config::hybrid_cutoff_scale (config.h:174), default 1.0 */
-    uint32_t reserved[8];
+    uint32_t force_wide_offsets;   /* 1: 64-bit out-list offsets even where 32 bits suffice (the path
+                                      graphs with nnz + 3n > 2^32 take; exposed for testing) */
+    uint32_t reserved[7];
 } ktri_opts;
 
 /* Counters of the last run on a context, named after the reference's Statistics fields

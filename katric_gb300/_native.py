@@ -47,7 +47,8 @@ class Opts(ctypes.Structure):
         ("collect_stats", ctypes.c_uint32),
         ("binary_intersection_cutoff", ctypes.c_uint64),
         ("hybrid_cutoff_scale", ctypes.c_double),
-        ("reserved", ctypes.c_uint32 * 8),
+        ("force_wide_offsets", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 7),
     ]
 
 

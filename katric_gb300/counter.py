@@ -53,6 +53,7 @@ class Config:
     per_vertex: bool = True
     collect_stats: bool = False
     device: int = 0
+    force_wide_offsets: bool = False
 
     def opts(self) -> _native.Opts:
         o = _native.Opts()
@@ -65,6 +66,7 @@ class Config:
         o.collect_stats = 1 if self.collect_stats else 0
         o.binary_intersection_cutoff = self.binary_intersection_cutoff
         o.hybrid_cutoff_scale = self.hybrid_cutoff_scale
+        o.force_wide_offsets = 1 if self.force_wide_offsets else 0
         return o
 
 

@@ -60,10 +60,11 @@ u64 isqrt_ceil(u64 x) {
 }
 
 // Workspace of one count.  num_sms = 0 sizes the grids for the largest supported part.
-Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs, bool internal_cnt) {
+Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs, bool internal_cnt,
+                   bool force_wide = false) {
     Layout L;
     const u64 cap = ktri::oriented_capacity(n, nnz);
-    L.wide = cap > 0xFFFFFFFFull;
+    L.wide = force_wide || cap > 0xFFFFFFFFull;
     const int sms = num_sms > 0 ? num_sms : 160;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -129,6 +130,7 @@ ktri::Options resolve(const ktri_opts* o) {
     r.collect_stats = o->collect_stats != 0;
     if (o->binary_intersection_cutoff) r.binary_cutoff = o->binary_intersection_cutoff;
     if (o->hybrid_cutoff_scale > 0) r.hybrid_scale = o->hybrid_cutoff_scale;
+    r.force_wide = o->force_wide_offsets != 0;
     return r;
 }
 
@@ -447,7 +449,7 @@ int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint
         ctx->stats = ktri_run_stats{};
         return KTRI_OK;
     }
-    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, false, d_per_vertex == nullptr);
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, false, d_per_vertex == nullptr, opt.force_wide);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex)
@@ -505,7 +507,7 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
     }
     if (first_out[0] != 0 || first_out[n] != nnz)
         return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
-    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true);
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->ws);
@@ -605,7 +607,7 @@ int ktri_count_batch_device(ktri_ctx* ctx, const uint64_t* d_first_out, const ui
         ctx->pending = false;
         return KTRI_OK;
     }
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true, opt.force_wide);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->ws);
@@ -641,7 +643,7 @@ int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_
     }
     if (first_out[0] != 0 || first_out[n_total] != nnz_total)
         return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, true, true);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, true, true, opt.force_wide);
     const size_t off_gf = L.bytes, off_tot = align_up(off_gf + sizeof(u64) * (num_graphs + 1));
     const size_t total_bytes = align_up(off_tot + sizeof(u64) * (num_graphs + 1));
     rc = ensure_ws(ctx, total_bytes);
@@ -695,7 +697,7 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
     if (n_total == 0) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "a plan needs at least one vertex");
     DeviceGuard g(ctx->device);
     if (ctx->pending) device_status(ctx);
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true, opt.force_wide);
     if (ctx->budget && L.bytes > ctx->budget)
         return set_error(ctx, KTRI_ERR_OUT_OF_MEMORY, "plan workspace exceeds the memory budget");
     ktri_plan* p = new (std::nothrow) ktri_plan();

@@ -22,6 +22,7 @@ struct Options {
     bool collect_stats = false;
     uint64_t binary_cutoff = 1000;
     double hybrid_scale = 1.0;
+    bool force_wide = false;
 };
 
 // Device-side error bits written by the kernels (one u32 word in the control block).

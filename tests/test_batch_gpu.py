@@ -19,11 +19,11 @@ def oracle_batch(oracle, b: Batch):
     return np.array(totals, dtype=np.uint64), np.concatenate(pvs)
 
 
-@pytest.mark.parametrize("method", ["auto", "merge"])
-def test_batch_parity(counter, oracle, method):
+@pytest.mark.parametrize("method,wide", [("auto", False), ("merge", False), ("auto", True)])
+def test_batch_parity(counter, oracle, method, wide):
     b = Batch.generate(60, 5, 12, 4, 40, seed=21)
     et, epv = oracle_batch(oracle, b)
-    totals, pv = counter.count_batch(b, Config(intersection_method=method))
+    totals, pv = counter.count_batch(b, Config(intersection_method=method, force_wide_offsets=wide))
     assert np.array_equal(totals, et)
     assert np.array_equal(pv, epv)
 

@@ -67,6 +67,15 @@ def test_rgg(counter, oracle, n):
     check_parity(counter, oracle, g.first_out, g.head)
 
 
+@pytest.mark.parametrize("method", ["auto", "merge"])
+def test_wide_offsets(counter, oracle, method):
+    """64-bit out-list offsets (the path of unions with nnz + 3n > 2^32), forced on small graphs."""
+    for g in (Graph.rmat(14, 16, seed=2), Graph.rgg2d(1 << 14, 32.0, seed=3), Graph.gnm(1 << 14, 1 << 17, seed=1)):
+        total, pv, _ = oracle.count(g.first_out, g.head, num_threads=8)
+        t, p = counter.count(g.first_out, g.head, Config(intersection_method=method, force_wide_offsets=True))
+        assert t == total and np.array_equal(p, pv)
+
+
 def test_unsorted_lists(counter, oracle):
     g = Graph.rmat(13, 16, seed=5)
     fo = g.first_out
