@@ -166,6 +166,37 @@ int ktri_plan_launch(ktri_plan* plan, void* stream);
 int ktri_plan_check(ktri_plan* plan);
 int ktri_plan_destroy(ktri_plan* plan);
 
+/* ---- serving ------------------------------------------------------------------------------
+ * No counterpart in the reference.  A request loop with continuous batching: requests (one
+ * graph each) queue up; a worker thread packs the waiting ones into a batch under the device
+ * memory budget and counts it on one of `slots` contexts, while batches already on the GPU
+ * keep running (their work overlaps).  Counted graphs stay resident (CSR and counts on the
+ * device, keyed by graph_key) until the budget needs their room; a request for a resident
+ * key is answered from the resident counts.  submit copies the caller's CSR (first_out may be
+ * NULL to repeat a resident key); wait blocks until the request is done and reports its
+ * latency (submit to completion). */
+typedef struct ktri_server ktri_server;
+typedef struct ktri_server_opts {
+    uint32_t struct_size;        /* sizeof(ktri_server_opts); 0 = defaults */
+    uint32_t slots;              /* batches in flight at once (default 2) */
+    uint64_t memory_budget;      /* device bytes for resident graphs and batches (default 120 GiB) */
+    uint64_t max_batch_nnz;      /* adjacency entries per batch (default 2^28) */
+    uint32_t max_batch_graphs;   /* graphs per batch (default 4096) */
+    uint32_t reserved[7];
+} ktri_server_opts;
+typedef struct ktri_server_stats {
+    uint64_t submitted, completed, batches, batched_graphs, cache_hits, evictions, resident_graphs, resident_bytes,
+        peak_inflight_batches;
+    uint64_t reserved[7];
+} ktri_server_stats;
+int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out);
+int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,
+                       uint64_t n, uint64_t nnz, int want_per_vertex, uint64_t* request_id);
+int ktri_server_wait(ktri_server* s, uint64_t request_id, uint64_t* total, uint64_t* per_vertex_out,
+                     double* latency_s);
+int ktri_server_get_stats(ktri_server* s, ktri_server_stats* out);
+int ktri_server_destroy(ktri_server* s);
+
 /* Oriented, id-sorted out-lists (the state of DistributedGraph after preprocessing,
  * shared_memory_cetric.h:72-103, restricted to out_adj, distributed_graph.h:512-514) as a
  * compact CSR: out_first_out[n+1] and out_head[nnz/2].  Host buffers; synchronous. */
@@ -202,6 +233,10 @@ int ktri_graph_read_metis(const char* path, ktri_graph** out);
 int ktri_graph_read_binary(const char* stem, ktri_graph** out);
 int ktri_graph_write_binary(const ktri_graph* g, const char* stem);
 int ktri_graph_write_metis(const ktri_graph* g, const char* path);
+/* Many graphs from explicit specs in parallel: kinds[i] 0 = G(n,m) (m = round(n d / 2)),
+ * 1 = RMAT (0.57, 0.19, 0.19) with round(n d / 2) draws, 2 = 2D RGG; outs[i] receives graph i. */
+int ktri_graphs_generate(uint64_t count, const uint32_t* kinds, const uint64_t* ns, const double* degrees,
+                         const uint64_t* seeds, ktri_graph** outs);
 uint64_t ktri_graph_n(const ktri_graph* g);
 uint64_t ktri_graph_nnz(const ktri_graph* g);
 const uint64_t* ktri_graph_first_out(const ktri_graph* g);

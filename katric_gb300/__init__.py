@@ -8,8 +8,9 @@ from ._native import KtriError, load
 from .counter import (Config, LocalStatistics, Plan, Statistics, TriangleCounter, default_counter, intersection,
                       preprocessing, run_shmem)
 from .graph import Batch, Graph, generate
+from .serve import Server
 
 __all__ = [
     "Batch", "Config", "Graph", "Plan", "KtriError", "LocalStatistics", "Statistics", "TriangleCounter", "default_counter",
-    "generate", "intersection", "load", "preprocessing", "run_shmem",
+    "generate", "intersection", "load", "preprocessing", "run_shmem", "Server",
 ]

@@ -52,6 +52,23 @@ class Opts(ctypes.Structure):
     ]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("slots", ctypes.c_uint32),
+        ("memory_budget", ctypes.c_uint64),
+        ("max_batch_nnz", ctypes.c_uint64),
+        ("max_batch_graphs", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 7),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "batches", "batched_graphs", "cache_hits",
+                                              "evictions", "resident_graphs", "resident_bytes",
+                                              "peak_inflight_batches")] + [("reserved", ctypes.c_uint64 * 7)]
+
+
 class RunStats(ctypes.Structure):
     _fields_ = [
         ("triangles", ctypes.c_uint64),
@@ -95,6 +112,11 @@ SIGNATURES = {
     "ktri_plan_launch": (ctypes.c_int, [P, P]),
     "ktri_plan_check": (ctypes.c_int, [P]),
     "ktri_plan_destroy": (ctypes.c_int, [P]),
+    "ktri_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServerOpts), PP]),
+    "ktri_server_submit": (ctypes.c_int, [P, U64, P, P, U64, U64, ctypes.c_int, ctypes.POINTER(U64)]),
+    "ktri_server_wait": (ctypes.c_int, [P, U64, ctypes.POINTER(U64), P, ctypes.POINTER(ctypes.c_double)]),
+    "ktri_server_get_stats": (ctypes.c_int, [P, ctypes.POINTER(ServerStats)]),
+    "ktri_server_destroy": (ctypes.c_int, [P]),
     "ktri_orient_csr": (ctypes.c_int, [P, P, P, U64, U64, P, P]),
     "ktri_intersect_pairs": (ctypes.c_int, [P, I32, P, P, P, P, U64, P, P]),
     "ktri_graph_from_csr": (ctypes.c_int, [U64, P, P, PP]),
@@ -104,6 +126,7 @@ SIGNATURES = {
     "ktri_graph_rgg2d": (ctypes.c_int, [U64, D, U64, PP]),
     "ktri_batch_pack": (ctypes.c_int, [U64, P, PP, P]),
     "ktri_batch_generate": (ctypes.c_int, [U64, D, D, D, D, U64, PP, P]),
+    "ktri_graphs_generate": (ctypes.c_int, [U64, P, P, P, P, P]),
     "ktri_graph_read_metis": (ctypes.c_int, [CP, PP]),
     "ktri_graph_read_binary": (ctypes.c_int, [CP, PP]),
     "ktri_graph_write_binary": (ctypes.c_int, [P, CP]),

@@ -514,6 +514,37 @@ int ktri_batch_generate(uint64_t num_graphs, double log2_n_min, double log2_n_ma
     return result;
 }
 
+// Many graphs from explicit specs, generated in parallel (one thread per graph): graph i is
+// kinds[i] = 0 G(n,m) with m = round(n d / 2), 1 RMAT with round(n d / 2) draws, 2 2D RGG
+// with average degree d; n = ns[i], d = degrees[i], seed = seeds[i].
+int ktri_graphs_generate(uint64_t count, const uint32_t* kinds, const uint64_t* ns, const double* degrees,
+                         const uint64_t* seeds, ktri_graph** outs) {
+    if (!outs || (count && (!kinds || !ns || !degrees || !seeds))) return KTRI_ERR_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < count; ++i) outs[i] = nullptr;
+    std::atomic<int> rc{KTRI_OK};
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t ii = 0; ii < (int64_t)count; ++ii) {
+        const uint64_t i = (uint64_t)ii, n = ns[i];
+        const double d = degrees[i];
+        const uint64_t half = (uint64_t)std::llround((double)n * d / 2.0);
+        int r;
+        switch (kinds[i]) {
+            case 0: r = ktri_graph_gnm(n, std::min(half, n * (n - 1) / 2), seeds[i], &outs[i]); break;
+            case 1: r = ktri_graph_rmat_n(n, half, 0.57, 0.19, 0.19, seeds[i], &outs[i]); break;
+            case 2: r = ktri_graph_rgg2d(n, d, seeds[i], &outs[i]); break;
+            default: r = KTRI_ERR_INVALID_ARGUMENT;
+        }
+        if (r != KTRI_OK) rc.store(r);
+    }
+    if (rc.load() != KTRI_OK) {
+        for (uint64_t i = 0; i < count; ++i) {
+            delete outs[i];
+            outs[i] = nullptr;
+        }
+    }
+    return rc.load();
+}
+
 uint64_t ktri_graph_n(const ktri_graph* g) { return g ? g->n : 0; }
 uint64_t ktri_graph_nnz(const ktri_graph* g) { return g ? g->head.size() : 0; }
 const uint64_t* ktri_graph_first_out(const ktri_graph* g) { return g ? g->first_out.data() : nullptr; }

@@ -1,0 +1,553 @@
+// Serving: a request loop that counts many graphs with continuous batching.
+//
+// Requests (one graph each) are queued by ktri_server_submit.  A worker thread forms a batch
+// from the waiting requests under a device-memory budget, packs the graphs as one disjoint
+// union (host staging -> device, ids rebased on the device), counts the whole batch with one
+// ktri_count_batch_device call on one of `slots` contexts (each with its own stream), and
+// reads back totals and per-vertex counts.  While one batch runs, the next one is formed from
+// the requests that arrived meanwhile and launched on a free slot, so the work of batches
+// overlaps on the GPU.  Graphs stay resident (CSR and counts on the device, keyed by the
+// caller's graph key) until the memory budget needs their room; a repeated request for a
+// resident graph is answered from the resident counts without counting again.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "ktri.h"
+#include "ktri_device.cuh"
+
+using ktri::u32;
+using ktri::u64;
+
+namespace {
+
+// Rebase a packed union: graph g's offsets were copied relative to its own start and its
+// ids relative to its own first vertex.
+__global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64* __restrict__ vfirst,
+                         const u64* __restrict__ efirst, u64 num_graphs) {
+    for (u64 g = blockIdx.x; g < num_graphs; g += gridDim.x) {
+        const u64 vb = vfirst[g], ve = vfirst[g + 1], eb = efirst[g], ee = efirst[g + 1];
+        for (u64 v = vb + 1 + threadIdx.x; v <= ve; v += blockDim.x) fo[v] += eb;
+        for (u64 e = eb + threadIdx.x; e < ee; e += blockDim.x) head[e] += (u32)vb;
+    }
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    uint64_t id = 0, key = 0;
+    std::vector<uint64_t> fo;
+    std::vector<uint32_t> head;
+    uint64_t n = 0, nnz = 0;
+    bool want_pv = false;
+    double t_submit = 0, t_done = 0;
+    bool done = false;
+    int status = KTRI_OK;
+    uint64_t total = 0;
+    std::vector<uint64_t> pv;
+};
+
+struct Resident {  // a graph kept on the device with its counts
+    uint64_t key = 0, n = 0, nnz = 0, total = 0;
+    void* mem = nullptr;  // [fo u64 n+1][head u32 nnz][pv u64 n]
+    size_t bytes = 0;
+    std::list<uint64_t>::iterator lru;
+};
+
+struct Slot {
+    ktri_ctx* ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaEvent_t cache_done = nullptr;  // resident copies out of this slot's buffers are finished
+    bool busy = false;
+    std::vector<Request*> reqs;
+    // device union buffers (grow-only)
+    void* dev = nullptr;
+    size_t dev_bytes = 0;
+    // pinned host staging (grow-only)
+    void* host = nullptr;
+    size_t host_bytes = 0;
+    u64 n_total = 0, nnz_total = 0;
+    size_t off_fo = 0, off_head = 0, off_vf = 0, off_ef = 0, off_tot = 0, off_pv = 0;
+    size_t h_tot = 0, h_pv = 0;
+};
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct ktri_server {
+    int device = 0;
+    ktri_server_opts opts{};
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request*> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
+    uint64_t next_id = 1;
+    bool stop = false;
+    std::thread worker;
+    std::vector<Slot> slots;
+    cudaStream_t aux = nullptr;  // cache copies
+    // resident graphs
+    std::unordered_map<uint64_t, Resident> resident;
+    std::list<uint64_t> lru;  // front = most recent
+    size_t resident_bytes = 0;
+    ktri_server_stats st{};
+    int fatal = KTRI_OK;
+};
+
+namespace {
+
+// Device bytes a batch of (n_total, nnz_total, k graphs) needs in a slot: union buffers plus
+// the counting workspace.
+size_t batch_bytes(u64 n, u64 nnz, u64 k) {
+    return al(8 * (n + 1)) + al(4 * (nnz + 1)) + 2 * al(8 * (k + 1)) + al(8 * k) + al(8 * (n + 1)) +
+           (size_t)ktri_workspace_bytes(n, nnz, KTRI_METHOD_AUTO);
+}
+
+// Evict least-recently-used resident graphs until `need` more bytes fit the budget.
+// Called with s->mu held.
+bool make_room(ktri_server* s, size_t need, size_t inflight) {
+    while (s->resident_bytes + inflight + need > s->opts.memory_budget && !s->lru.empty()) {
+        const uint64_t key = s->lru.back();
+        s->lru.pop_back();
+        auto it = s->resident.find(key);
+        if (it != s->resident.end()) {
+            cudaFreeAsync(it->second.mem, s->aux);
+            s->resident_bytes -= it->second.bytes;
+            s->resident.erase(it);
+            s->st.evictions++;
+        }
+    }
+    return s->resident_bytes + inflight + need <= s->opts.memory_budget;
+}
+
+void finish(ktri_server* s, Request* r, int status) {
+    r->status = status;
+    r->t_done = now_s();
+    r->done = true;
+    s->st.completed++;
+}
+
+// Answer a request for a resident graph from its resident counts.
+void serve_resident(ktri_server* s, Request* r, Resident& res) {
+    r->total = res.total;
+    if (r->want_pv && res.n) {
+        r->pv.resize(res.n);
+        const char* base = static_cast<const char*>(res.mem);
+        const size_t off_pv = al(8 * (res.n + 1)) + al(4 * (res.nnz + 1));
+        cudaMemcpyAsync(r->pv.data(), base + off_pv, 8 * res.n, cudaMemcpyDeviceToHost, s->aux);
+        cudaStreamSynchronize(s->aux);
+    }
+    s->lru.erase(res.lru);
+    s->lru.push_front(res.key);
+    res.lru = s->lru.begin();
+    s->st.cache_hits++;
+}
+
+// Keep a counted graph resident (CSR + counts on the device), room permitting.
+void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 ebase, size_t inflight) {
+    if (!r->key || s->resident.count(r->key)) return;
+    const size_t bytes = al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)) + al(8 * (r->n + 1));
+    if (bytes > s->opts.memory_budget / 4) return;
+    if (!make_room(s, bytes, inflight)) return;
+    void* mem = nullptr;
+    if (cudaMallocAsync(&mem, bytes, s->aux) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    char* b = static_cast<char*>(mem);
+    const char* d = static_cast<const char*>(sl.dev);
+    // the slot's union holds rebased ids; the resident copy keeps the caller's own CSR
+    cudaMemcpyAsync(b, r->fo.data(), 8 * (r->n + 1), cudaMemcpyHostToDevice, s->aux);
+    if (r->nnz) cudaMemcpyAsync(b + al(8 * (r->n + 1)), r->head.data(), 4 * r->nnz, cudaMemcpyHostToDevice, s->aux);
+    cudaMemcpyAsync(b + al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)), d + sl.off_pv + 8 * vbase, 8 * r->n,
+                    cudaMemcpyDeviceToDevice, s->aux);
+    (void)ebase;
+    Resident res;
+    res.key = r->key;
+    res.n = r->n;
+    res.nnz = r->nnz;
+    res.total = r->total;
+    res.mem = mem;
+    res.bytes = bytes;
+    s->lru.push_front(r->key);
+    res.lru = s->lru.begin();
+    s->resident_bytes += bytes;
+    s->resident.emplace(r->key, res);
+}
+
+int grow(void** p, size_t* have, size_t need, bool host) {
+    if (need <= *have) return KTRI_OK;
+    if (*p) {
+        cudaDeviceSynchronize();  // nothing may still read the old buffer
+        if (host) cudaFreeHost(*p);
+        else cudaFree(*p);
+        *p = nullptr;
+        *have = 0;
+    }
+    const size_t want = need + need / 4;
+    cudaError_t e = host ? cudaHostAlloc(p, want, cudaHostAllocDefault) : cudaMalloc(p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return KTRI_ERR_OUT_OF_MEMORY;
+    }
+    *have = want;
+    return KTRI_OK;
+}
+
+// Pack the slot's requests and launch their count.  Called without the lock.
+int launch_batch(ktri_server* s, Slot& sl) {
+    const u64 k = sl.reqs.size();
+    u64 n = 0, nnz = 0;
+    for (Request* r : sl.reqs) {
+        n += r->n;
+        nnz += r->nnz;
+    }
+    sl.n_total = n;
+    sl.nnz_total = nnz;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t at = off;
+        off = al(off + b);
+        return at;
+    };
+    sl.off_fo = take(8 * (n + 1));
+    sl.off_head = take(4 * (nnz + 1));
+    sl.off_vf = take(8 * (k + 1));
+    sl.off_ef = take(8 * (k + 1));
+    sl.off_tot = take(8 * k);
+    sl.off_pv = take(8 * (n + 1));
+    int rc = grow(&sl.dev, &sl.dev_bytes, off, false);
+    if (rc) return rc;
+    // host staging: [fo][head][vf][ef] then read-back [tot][pv]
+    size_t hoff = 0;
+    auto htake = [&](size_t b) {
+        size_t at = hoff;
+        hoff = al(hoff + b);
+        return at;
+    };
+    const size_t h_fo = htake(8 * (n + 1)), h_head = htake(4 * (nnz + 1)), h_vf = htake(8 * (k + 1)),
+                 h_ef = htake(8 * (k + 1));
+    sl.h_tot = htake(8 * k);
+    sl.h_pv = htake(8 * (n + 1));
+    rc = grow(&sl.host, &sl.host_bytes, hoff, true);
+    if (rc) return rc;
+    char* h = static_cast<char*>(sl.host);
+    u64* hfo = reinterpret_cast<u64*>(h + h_fo);
+    u32* hhead = reinterpret_cast<u32*>(h + h_head);
+    u64* hvf = reinterpret_cast<u64*>(h + h_vf);
+    u64* hef = reinterpret_cast<u64*>(h + h_ef);
+    hfo[0] = 0;
+    u64 vb = 0, eb = 0;
+    for (u64 i = 0; i < k; ++i) {
+        Request* r = sl.reqs[i];
+        hvf[i] = vb;
+        hef[i] = eb;
+        std::memcpy(hfo + vb + 1, r->fo.data() + 1, 8 * r->n);
+        if (r->nnz) std::memcpy(hhead + eb, r->head.data(), 4 * r->nnz);
+        vb += r->n;
+        eb += r->nnz;
+    }
+    hvf[k] = vb;
+    hef[k] = eb;
+    char* d = static_cast<char*>(sl.dev);
+    cudaStream_t st = sl.stream;
+    cudaStreamWaitEvent(st, sl.cache_done, 0);  // earlier resident copies read these buffers
+    cudaMemcpyAsync(d + sl.off_fo, hfo, 8 * (n + 1), cudaMemcpyHostToDevice, st);
+    if (nnz) cudaMemcpyAsync(d + sl.off_head, hhead, 4 * nnz, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d + sl.off_vf, hvf, 8 * (k + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d + sl.off_ef, hef, 8 * (k + 1), cudaMemcpyHostToDevice, st);
+    auto* dfo = reinterpret_cast<u64*>(d + sl.off_fo);
+    auto* dhead = reinterpret_cast<u32*>(d + sl.off_head);
+    auto* dvf = reinterpret_cast<u64*>(d + sl.off_vf);
+    auto* def = reinterpret_cast<u64*>(d + sl.off_ef);
+    const unsigned blocks = (unsigned)std::min<u64>(k, 4096);
+    k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k);
+    if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
+    ktri_opts o{};
+    o.struct_size = sizeof(ktri_opts);
+    o.intersection_method = KTRI_METHOD_AUTO;
+    rc = ktri_count_batch_device(sl.ctx, reinterpret_cast<const uint64_t*>(dfo), dhead, n, nnz,
+                                 reinterpret_cast<const uint64_t*>(dvf), k, reinterpret_cast<uint64_t*>(d + sl.off_tot),
+                                 reinterpret_cast<uint64_t*>(d + sl.off_pv), &o, st);
+    if (rc) return rc;
+    cudaMemcpyAsync(h + sl.h_tot, d + sl.off_tot, 8 * k, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(sl.done, st);
+    return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
+}
+
+// Harvest a finished slot (called with the lock held).
+void harvest(ktri_server* s, Slot& sl) {
+    int rc = ktri_ctx_check(sl.ctx);
+    const char* h = static_cast<const char*>(sl.host);
+    const u64* tot = reinterpret_cast<const u64*>(h + sl.h_tot);
+    const u64* pv = reinterpret_cast<const u64*>(h + sl.h_pv);
+    size_t inflight = 0;
+    for (const Slot& o : s->slots) inflight += o.dev_bytes;
+    u64 vb = 0, eb = 0;
+    for (size_t i = 0; i < sl.reqs.size(); ++i) {
+        Request* r = sl.reqs[i];
+        if (rc == KTRI_OK) {
+            r->total = tot[i];
+            if (r->want_pv) r->pv.assign(pv + vb, pv + vb + r->n);
+            keep_resident(s, r, sl, vb, eb, inflight);
+        }
+        vb += r->n;
+        eb += r->nnz;
+        finish(s, r, rc);
+        r->fo.clear();
+        r->fo.shrink_to_fit();
+        r->head.clear();
+        r->head.shrink_to_fit();
+    }
+    cudaEventRecord(sl.cache_done, s->aux);
+    sl.reqs.clear();
+    sl.busy = false;
+}
+
+void worker_main(ktri_server* s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lock(s->mu);
+    while (true) {
+        // finished batches
+        bool any_busy = false;
+        for (Slot& sl : s->slots) {
+            if (sl.busy && cudaEventQuery(sl.done) == cudaSuccess) {
+                harvest(s, sl);
+                s->cv_done.notify_all();
+            }
+            any_busy |= sl.busy;
+        }
+        if (s->stop && s->pending.empty() && !any_busy) break;
+        // requests for resident graphs are answered at once
+        for (auto it = s->pending.begin(); it != s->pending.end();) {
+            Request* r = *it;
+            auto res = r->key ? s->resident.find(r->key) : s->resident.end();
+            if (res != s->resident.end()) {
+                serve_resident(s, r, res->second);
+                finish(s, r, KTRI_OK);
+                it = s->pending.erase(it);
+                s->cv_done.notify_all();
+            } else if (r->fo.empty()) {  // a repeat by key of a graph that is no longer resident
+                finish(s, r, KTRI_ERR_INVALID_ARGUMENT);
+                it = s->pending.erase(it);
+                s->cv_done.notify_all();
+            } else {
+                ++it;
+            }
+        }
+        // admit a batch into a free slot
+        Slot* free_slot = nullptr;
+        for (Slot& sl : s->slots)
+            if (!sl.busy) {
+                free_slot = &sl;
+                break;
+            }
+        if (free_slot && !s->pending.empty()) {
+            std::vector<Request*> batch;
+            u64 n = 0, nnz = 0;
+            size_t inflight = 0;
+            for (const Slot& o : s->slots)
+                if (&o != free_slot) inflight += o.dev_bytes;
+            while (!s->pending.empty() && batch.size() < s->opts.max_batch_graphs) {
+                Request* r = s->pending.front();
+                const u64 n2 = n + r->n, nnz2 = nnz + r->nnz;
+                if (!batch.empty() && (nnz2 > s->opts.max_batch_nnz || n2 > 0x7FFFFFFFull)) break;
+                if (!batch.empty() && batch_bytes(n2, nnz2, batch.size() + 1) + inflight + s->resident_bytes >
+                                          s->opts.memory_budget)
+                    break;
+                batch.push_back(r);
+                s->pending.pop_front();
+                n = n2;
+                nnz = nnz2;
+            }
+            const size_t need = batch_bytes(n, nnz, batch.size());
+            make_room(s, need > free_slot->dev_bytes ? need - free_slot->dev_bytes : 0, inflight + free_slot->dev_bytes);
+            if (need + inflight > s->opts.memory_budget || n > 0xFFFFFFFFull) {
+                for (Request* r : batch) finish(s, r, KTRI_ERR_OUT_OF_MEMORY);
+                s->cv_done.notify_all();
+            } else {
+                free_slot->reqs = batch;
+                free_slot->busy = true;
+                s->st.batches++;
+                s->st.batched_graphs += batch.size();
+                lock.unlock();
+                const int rc = launch_batch(s, *free_slot);
+                lock.lock();
+                if (rc) {
+                    cudaStreamSynchronize(free_slot->stream);
+                    for (Request* r : free_slot->reqs) finish(s, r, rc);
+                    free_slot->reqs.clear();
+                    free_slot->busy = false;
+                    s->cv_done.notify_all();
+                }
+                u64 busy = 0;
+                for (const Slot& o : s->slots) busy += o.busy;
+                s->st.peak_inflight_batches = std::max<u64>(s->st.peak_inflight_batches, busy);
+            }
+            continue;
+        }
+        // nothing to start: wait briefly for new requests or a finishing batch
+        s->cv_work.wait_for(lock, std::chrono::microseconds(any_busy ? 50 : 2000));
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out) {
+    if (!out) return KTRI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return KTRI_ERR_NO_DEVICE;
+    }
+    ktri_server* s = new (std::nothrow) ktri_server();
+    if (!s) return KTRI_ERR_OUT_OF_MEMORY;
+    s->device = device;
+    s->opts.struct_size = sizeof(ktri_server_opts);
+    s->opts.slots = 2;
+    s->opts.memory_budget = 120ull << 30;
+    s->opts.max_batch_nnz = 1ull << 28;
+    s->opts.max_batch_graphs = 4096;
+    if (opts && opts->struct_size) {
+        if (opts->slots) s->opts.slots = opts->slots;
+        if (opts->memory_budget) s->opts.memory_budget = opts->memory_budget;
+        if (opts->max_batch_nnz) s->opts.max_batch_nnz = opts->max_batch_nnz;
+        if (opts->max_batch_graphs) s->opts.max_batch_graphs = opts->max_batch_graphs;
+    }
+    if (s->opts.slots > 8) s->opts.slots = 8;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    s->slots.resize(s->opts.slots);
+    int rc = KTRI_OK;
+    for (Slot& sl : s->slots) {
+        rc = ktri_ctx_create(device, &sl.ctx);
+        if (rc) break;
+        cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&sl.cache_done, cudaEventDisableTiming);
+    }
+    cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+    cudaSetDevice(prev);
+    if (rc) {
+        for (Slot& sl : s->slots)
+            if (sl.ctx) ktri_ctx_destroy(sl.ctx);
+        delete s;
+        return rc;
+    }
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return KTRI_OK;
+}
+
+int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,
+                       uint64_t n, uint64_t nnz, int want_per_vertex, uint64_t* request_id) {
+    if (!s || !request_id) return KTRI_ERR_INVALID_ARGUMENT;
+    auto r = std::make_unique<Request>();
+    r->key = graph_key;
+    r->want_pv = want_per_vertex != 0;
+    if (first_out) {
+        if (n > 0x7FFFFFFFull) return KTRI_ERR_UNSUPPORTED;
+        if (first_out[0] != 0 || first_out[n] != nnz || (nnz && !head)) return KTRI_ERR_INVALID_CSR;
+        r->n = n;
+        r->nnz = nnz;
+        r->fo.assign(first_out, first_out + n + 1);
+        r->head.assign(head, head + nnz);
+        for (uint64_t v = 0; v < n; ++v)
+            if (first_out[v + 1] < first_out[v]) return KTRI_ERR_INVALID_CSR;
+    } else if (!graph_key) {
+        return KTRI_ERR_INVALID_ARGUMENT;  // a repeat by key needs a key
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->stop) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!first_out && !s->resident.count(graph_key)) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!first_out) {
+        const Resident& res = s->resident.at(graph_key);
+        r->n = res.n;
+        r->nnz = res.nnz;
+    }
+    r->id = s->next_id++;
+    r->t_submit = now_s();
+    *request_id = r->id;
+    s->pending.push_back(r.get());
+    s->requests.emplace(r->id, std::move(r));
+    s->st.submitted++;
+    s->cv_work.notify_one();
+    return KTRI_OK;
+}
+
+int ktri_server_wait(ktri_server* s, uint64_t request_id, uint64_t* total, uint64_t* per_vertex_out,
+                     double* latency_s) {
+    if (!s) return KTRI_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lock(s->mu);
+    auto it = s->requests.find(request_id);
+    if (it == s->requests.end()) return KTRI_ERR_INVALID_ARGUMENT;
+    Request* r = it->second.get();
+    s->cv_done.wait(lock, [&] { return r->done; });
+    const int status = r->status;
+    if (status == KTRI_OK) {
+        if (total) *total = r->total;
+        if (per_vertex_out && r->want_pv && r->n) std::memcpy(per_vertex_out, r->pv.data(), 8 * r->n);
+    }
+    if (latency_s) *latency_s = r->t_done - r->t_submit;
+    s->requests.erase(it);
+    return status;
+}
+
+int ktri_server_get_stats(ktri_server* s, ktri_server_stats* out) {
+    if (!s || !out) return KTRI_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(s->mu);
+    *out = s->st;
+    out->resident_graphs = s->resident.size();
+    out->resident_bytes = s->resident_bytes;
+    return KTRI_OK;
+}
+
+int ktri_server_destroy(ktri_server* s) {
+    if (!s) return KTRI_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    for (auto& kv : s->resident) cudaFreeAsync(kv.second.mem, s->aux);
+    cudaStreamSynchronize(s->aux);
+    for (Slot& sl : s->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.cache_done) cudaEventDestroy(sl.cache_done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.ctx) ktri_ctx_destroy(sl.ctx);
+    }
+    if (s->aux) cudaStreamDestroy(s->aux);
+    cudaSetDevice(prev);
+    delete s;
+    return KTRI_OK;
+}
+
+}  // extern "C"

@@ -137,6 +137,20 @@ class Graph:
         _native.check(_native.load().ktri_graph_write_metis(self._native_handle(), path.encode()))
 
 
+def generate_many(kinds, ns, degrees, seeds) -> list[Graph]:
+    """Graphs from explicit specs, generated in parallel on the host (one thread per graph).
+    kinds: 0 = G(n,m) with m = round(n d / 2), 1 = RMAT with round(n d / 2) draws, 2 = 2D RGG."""
+    k = len(kinds)
+    kinds = np.ascontiguousarray(kinds, dtype=np.uint32)
+    ns = np.ascontiguousarray(ns, dtype=np.uint64)
+    degrees = np.ascontiguousarray(degrees, dtype=np.float64)
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    outs = (ctypes.c_void_p * max(1, k))()
+    _native.check(_native.load().ktri_graphs_generate(k, kinds.ctypes.data, ns.ctypes.data, degrees.ctypes.data,
+                                                      seeds.ctypes.data, outs))
+    return [Graph._from_handle(ctypes.c_void_p(outs[i])) for i in range(k)]
+
+
 def generate(name: str, seed: int | None = None, **kw) -> Graph:
     """Named generator (the subset of --gen the engine is measured on): gnm, rmat, rgg2d."""
     name = name.lower()

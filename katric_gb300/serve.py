@@ -1,0 +1,87 @@
+"""Serving: the continuous-batching request loop of libktri.so (ktri_server_*).
+
+    with Server(memory_budget=120 << 30) as srv:
+        rid = srv.submit(graph, key=17)          # copies the CSR; key makes the graph resident
+        total, per_vertex, latency = srv.wait(rid)
+        rid = srv.submit(None, key=17)           # repeat of a resident graph: no CSR needed
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import numpy as np
+
+from . import _native
+from .graph import Graph
+
+
+class Server:
+    def __init__(self, device: int = 0, slots: int = 2, memory_budget: int = 120 << 30,
+                 max_batch_nnz: int = 1 << 28, max_batch_graphs: int = 4096):
+        self._L = _native.load()
+        o = _native.ServerOpts()
+        o.struct_size = ctypes.sizeof(_native.ServerOpts)
+        o.slots = slots
+        o.memory_budget = memory_budget
+        o.max_batch_nnz = max_batch_nnz
+        o.max_batch_graphs = max_batch_graphs
+        h = ctypes.c_void_p()
+        _native.check(self._L.ktri_server_create(device, ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._meta: dict[int, tuple[int, bool]] = {}
+        self._mu = threading.Lock()
+        self._sizes: dict[int, int] = {}  # key -> n of the graph last submitted under it
+
+    def submit(self, graph: Graph | None, key: int = 0, per_vertex: bool = True) -> int:
+        rid = ctypes.c_uint64(0)
+        if graph is None:
+            if not key:
+                raise ValueError("a repeat needs the key of a resident graph")
+            rc = self._L.ktri_server_submit(self._h, key, None, None, 0, 0, int(per_vertex), ctypes.byref(rid))
+            n = self._sizes.get(key, 0)
+        else:
+            rc = self._L.ktri_server_submit(self._h, key, graph.first_out.ctypes.data,
+                                            graph.head.ctypes.data if graph.nnz else None, graph.n, graph.nnz,
+                                            int(per_vertex), ctypes.byref(rid))
+            n = graph.n
+        _native.check(rc)
+        with self._mu:
+            self._meta[rid.value] = (n, per_vertex)
+            if graph is not None and key:
+                self._sizes[key] = graph.n
+        return rid.value
+
+    def wait(self, rid: int):
+        """(total, per-vertex counts or None, latency in seconds)."""
+        with self._mu:
+            n, want = self._meta.pop(rid)
+        total = ctypes.c_uint64(0)
+        lat = ctypes.c_double(0)
+        pv = np.zeros(max(1, n), dtype=np.uint64) if want else None
+        rc = self._L.ktri_server_wait(self._h, rid, ctypes.byref(total), pv.ctypes.data if pv is not None else None,
+                                      ctypes.byref(lat))
+        _native.check(rc)
+        return int(total.value), (pv[:n] if pv is not None else None), float(lat.value)
+
+    def stats(self) -> dict:
+        st = _native.ServerStats()
+        _native.check(self._L.ktri_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: int(getattr(st, k)) for k, _ in _native.ServerStats._fields_ if k != "reserved"}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self._L.ktri_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

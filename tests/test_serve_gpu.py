@@ -1,0 +1,71 @@
+"""Serving with continuous batching (needs a GB300): every result is the same alone and in
+the mix, repeats are answered from resident graphs, the memory budget is honoured."""
+import threading
+
+import numpy as np
+import pytest
+
+from katric_gb300 import Batch, Graph, KtriError, Server, TriangleCounter, _native
+
+pytestmark = pytest.mark.gpu
+
+
+def graph_mix(count, seed):
+    b = Batch.generate(count, 6, 14, 4, 48, seed=seed)
+    return [b.graph(i) for i in range(b.num_graphs)]
+
+
+def test_results_alone_equal_results_in_the_mix():
+    graphs = graph_mix(90, seed=31) + [Graph.rmat(15, 16, seed=3), Graph(np.zeros(5, np.uint64),
+                                                                          np.zeros(0, np.uint32))]
+    with TriangleCounter(0) as ctr:
+        alone = [ctr.count(g.first_out, g.head) for g in graphs]
+    with Server(slots=2, max_batch_nnz=1 << 18) as srv:
+        rids = [None] * len(graphs)
+
+        def client(lo, hi):
+            for i in range(lo, hi):
+                rids[i] = srv.submit(graphs[i], key=1000 + i)
+
+        threads = [threading.Thread(target=client, args=(k * 23, min(len(graphs), (k + 1) * 23))) for k in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        for i, g in enumerate(graphs):
+            total, pv, lat = srv.wait(rids[i])
+            assert total == alone[i][0], i
+            assert np.array_equal(pv, alone[i][1]), i
+            assert lat >= 0
+        st = srv.stats()
+        assert st["completed"] == len(graphs)
+        assert st["batches"] >= 2 and st["batched_graphs"] == len(graphs)
+        assert st["batches"] < len(graphs)  # requests were batched together
+        # repeats of resident graphs by key: answered from the resident counts
+        reps = [srv.submit(None, key=1000 + i) for i in range(0, len(graphs), 7)]
+        for j, rid in zip(range(0, len(graphs), 7), reps):
+            total, pv, _ = srv.wait(rid)
+            assert total == alone[j][0] and np.array_equal(pv, alone[j][1])
+        assert srv.stats()["cache_hits"] == len(reps)
+
+
+def test_memory_budget_evicts_and_refuses():
+    graphs = graph_mix(30, seed=5)
+    with TriangleCounter(0) as ctr:
+        alone = [ctr.count(g.first_out, g.head)[0] for g in graphs]
+    big = Graph.rmat(16, 16, seed=1)
+    budget = 96 << 20
+    with Server(slots=1, memory_budget=budget, max_batch_nnz=1 << 16) as srv:
+        for rnd in range(2):  # the second round re-submits with CSRs: evicted graphs are counted again
+            rids = [srv.submit(g, key=1 + i) for i, g in enumerate(graphs)]
+            for i, rid in enumerate(rids):
+                assert srv.wait(rid)[0] == alone[i]
+        st = srv.stats()
+        assert st["resident_bytes"] <= budget
+        rid = srv.submit(Graph.rmat(20, 16, seed=2), key=0, per_vertex=False)
+        with pytest.raises(KtriError) as e:  # its batch alone needs more than the budget
+            srv.wait(rid)
+        assert e.value.code == _native.ERR_OUT_OF_MEMORY
+        rid = srv.submit(big, key=0)
+        with TriangleCounter(0) as ctr:
+            assert srv.wait(rid)[0] == ctr.count(big.first_out, big.head)[0]
