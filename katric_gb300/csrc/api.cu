@@ -142,8 +142,7 @@ int ensure_ws(ktri_ctx* ctx, size_t bytes) {
     if (bytes <= ctx->ws_bytes) return KTRI_OK;
     if (ctx->ws) {
         KTRI_CK(ctx, cudaStreamSynchronize(ctx->stream));
-        if (ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
-        cudaFree(ctx->ws);
+        cudaFree(ctx->ws);  // waits for the work still using the old workspace
         ctx->ws = nullptr;
         ctx->ws_bytes = 0;
     }
@@ -261,7 +260,10 @@ int check_common(ktri_ctx* ctx, const void* fo, const void* head, u64 n, u64 nnz
 
 int device_status(ktri_ctx* ctx) {
     if (!ctx->pending) return KTRI_OK;
-    KTRI_CK(ctx, cudaStreamSynchronize(ctx->last_stream));
+    // The context's own stream also carries the host entry points' read-backs; a caller's
+    // stream is waited for through the end-of-call event (the stream may be gone by now).
+    if (ctx->last_stream == ctx->stream) KTRI_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    else KTRI_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
     Control h;
     KTRI_CK(ctx, cudaMemcpy(&h, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost));
     ctx->pending = false;
@@ -393,9 +395,10 @@ int ktri_ctx_create(int device, ktri_ctx** out) {
 int ktri_ctx_destroy(ktri_ctx* ctx) {
     if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
     {
+        // The caller's streams are not touched here (one may already be destroyed); freeing the
+        // workspace waits for the work still using it.
         DeviceGuard g(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-        if (ctx->last_stream && ctx->last_stream != ctx->stream) cudaStreamSynchronize(ctx->last_stream);
         if (ctx->ws) cudaFree(ctx->ws);
         for (auto& e : ctx->ev)
             if (e) cudaEventDestroy(e);
@@ -571,6 +574,7 @@ int enqueue_batch(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, con
     if (rc) return rc;
     ktri::launch_graph_totals(cnt, graph_first, num_graphs, n, totals, reinterpret_cast<Control*>(base + L.ctl),
                               ctx->num_sms, st);
+    if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[3], st));  // the call ends after the totals
     KTRI_CK(ctx, cudaGetLastError());
     return KTRI_OK;
 }

@@ -537,12 +537,12 @@ int ktri_server_destroy(ktri_server* s) {
     cudaStreamSynchronize(s->aux);
     for (Slot& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.ctx) ktri_ctx_destroy(sl.ctx);  // before the stream it last ran on goes away
         if (sl.dev) cudaFree(sl.dev);
         if (sl.host) cudaFreeHost(sl.host);
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.cache_done) cudaEventDestroy(sl.cache_done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
-        if (sl.ctx) ktri_ctx_destroy(sl.ctx);
     }
     if (s->aux) cudaStreamDestroy(s->aux);
     cudaSetDevice(prev);
