@@ -321,7 +321,7 @@ def run_serve(args):
                         time.sleep(delay)
                 # a repeat of a graph that was already submitted goes by key (resident graphs are
                 # answered from their counts; others are counted again from the CSR)
-                rids[i] = srv.submit(graphs[j], key=1 + j)
+                rids[i] = srv.submit(graphs[j], key=1 + j, borrow=True)
             done.set()
 
         th = threading.Thread(target=submitter)

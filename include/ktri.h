@@ -172,9 +172,12 @@ int ktri_plan_destroy(ktri_plan* plan);
  * memory budget and counts it on one of `slots` contexts, while batches already on the GPU
  * keep running (their work overlaps).  Counted graphs stay resident (CSR and counts on the
  * device, keyed by graph_key) until the budget needs their room; a request for a resident
- * key is answered from the resident counts.  submit copies the caller's CSR (first_out may be
- * NULL to repeat a resident key); wait blocks until the request is done and reports its
- * latency (submit to completion). */
+ * key is answered from the resident counts.  submit copies the caller's CSR, or with
+ * KTRI_SUBMIT_BORROW reads it in place (the caller keeps it alive and unchanged until wait
+ * returns); first_out may be NULL to repeat a resident key.  wait blocks until the request is
+ * done and reports its latency (submit to completion). */
+#define KTRI_SUBMIT_PER_VERTEX 1u /* return per-vertex counts */
+#define KTRI_SUBMIT_BORROW 2u     /* read the caller's CSR in place instead of copying it */
 typedef struct ktri_server ktri_server;
 typedef struct ktri_server_opts {
     uint32_t struct_size;        /* sizeof(ktri_server_opts); 0 = defaults */
@@ -191,7 +194,7 @@ typedef struct ktri_server_stats {
 } ktri_server_stats;
 int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out);
 int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,
-                       uint64_t n, uint64_t nnz, int want_per_vertex, uint64_t* request_id);
+                       uint64_t n, uint64_t nnz, uint32_t flags, uint64_t* request_id);
 int ktri_server_wait(ktri_server* s, uint64_t request_id, uint64_t* total, uint64_t* per_vertex_out,
                      double* latency_s);
 int ktri_server_get_stats(ktri_server* s, ktri_server_stats* out);

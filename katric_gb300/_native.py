@@ -113,7 +113,7 @@ SIGNATURES = {
     "ktri_plan_check": (ctypes.c_int, [P]),
     "ktri_plan_destroy": (ctypes.c_int, [P]),
     "ktri_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServerOpts), PP]),
-    "ktri_server_submit": (ctypes.c_int, [P, U64, P, P, U64, U64, ctypes.c_int, ctypes.POINTER(U64)]),
+    "ktri_server_submit": (ctypes.c_int, [P, U64, P, P, U64, U64, U32, ctypes.POINTER(U64)]),
     "ktri_server_wait": (ctypes.c_int, [P, U64, ctypes.POINTER(U64), P, ctypes.POINTER(ctypes.c_double)]),
     "ktri_server_get_stats": (ctypes.c_int, [P, ctypes.POINTER(ServerStats)]),
     "ktri_server_destroy": (ctypes.c_int, [P]),

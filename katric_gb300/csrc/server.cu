@@ -49,8 +49,10 @@ double now_s() {
 
 struct Request {
     uint64_t id = 0, key = 0;
-    std::vector<uint64_t> fo;
+    std::vector<uint64_t> fo;  // the copied CSR (empty when borrowed)
     std::vector<uint32_t> head;
+    const uint64_t* bfo = nullptr;  // the caller's CSR, read in place (borrowed or copied)
+    const uint32_t* bhead = nullptr;
     uint64_t n = 0, nnz = 0;
     bool want_pv = false;
     double t_submit = 0, t_done = 0;
@@ -172,8 +174,8 @@ void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 eb
     char* b = static_cast<char*>(mem);
     const char* d = static_cast<const char*>(sl.dev);
     // the slot's union holds rebased ids; the resident copy keeps the caller's own CSR
-    cudaMemcpyAsync(b, r->fo.data(), 8 * (r->n + 1), cudaMemcpyHostToDevice, s->aux);
-    if (r->nnz) cudaMemcpyAsync(b + al(8 * (r->n + 1)), r->head.data(), 4 * r->nnz, cudaMemcpyHostToDevice, s->aux);
+    cudaMemcpyAsync(b, r->bfo, 8 * (r->n + 1), cudaMemcpyHostToDevice, s->aux);
+    if (r->nnz) cudaMemcpyAsync(b + al(8 * (r->n + 1)), r->bhead, 4 * r->nnz, cudaMemcpyHostToDevice, s->aux);
     cudaMemcpyAsync(b + al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)), d + sl.off_pv + 8 * vbase, 8 * r->n,
                     cudaMemcpyDeviceToDevice, s->aux);
     (void)ebase;
@@ -257,13 +259,18 @@ int launch_batch(ktri_server* s, Slot& sl) {
         Request* r = sl.reqs[i];
         hvf[i] = vb;
         hef[i] = eb;
-        std::memcpy(hfo + vb + 1, r->fo.data() + 1, 8 * r->n);
-        if (r->nnz) std::memcpy(hhead + eb, r->head.data(), 4 * r->nnz);
         vb += r->n;
         eb += r->nnz;
     }
     hvf[k] = vb;
     hef[k] = eb;
+    // pack the graphs into pinned staging in parallel (ids are rebased on the device)
+#pragma omp parallel for schedule(dynamic, 1) if (k > 1 && nnz > (1u << 16))
+    for (int64_t ii = 0; ii < (int64_t)k; ++ii) {
+        const Request* r = sl.reqs[(size_t)ii];
+        std::memcpy(hfo + hvf[ii] + 1, r->bfo + 1, 8 * r->n);
+        if (r->nnz) std::memcpy(hhead + hef[ii], r->bhead, 4 * r->nnz);
+    }
     char* d = static_cast<char*>(sl.dev);
     cudaStream_t st = sl.stream;
     cudaStreamWaitEvent(st, sl.cache_done, 0);  // earlier resident copies read these buffers
@@ -343,7 +350,7 @@ void worker_main(ktri_server* s) {
                 finish(s, r, KTRI_OK);
                 it = s->pending.erase(it);
                 s->cv_done.notify_all();
-            } else if (r->fo.empty()) {  // a repeat by key of a graph that is no longer resident
+            } else if (!r->bfo) {  // a repeat by key of a graph that is no longer resident
                 finish(s, r, KTRI_ERR_INVALID_ARGUMENT);
                 it = s->pending.erase(it);
                 s->cv_done.notify_all();
@@ -460,20 +467,27 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
 }
 
 int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,
-                       uint64_t n, uint64_t nnz, int want_per_vertex, uint64_t* request_id) {
+                       uint64_t n, uint64_t nnz, uint32_t flags, uint64_t* request_id) {
     if (!s || !request_id) return KTRI_ERR_INVALID_ARGUMENT;
     auto r = std::make_unique<Request>();
     r->key = graph_key;
-    r->want_pv = want_per_vertex != 0;
+    r->want_pv = (flags & KTRI_SUBMIT_PER_VERTEX) != 0;
     if (first_out) {
         if (n > 0x7FFFFFFFull) return KTRI_ERR_UNSUPPORTED;
         if (first_out[0] != 0 || first_out[n] != nnz || (nnz && !head)) return KTRI_ERR_INVALID_CSR;
-        r->n = n;
-        r->nnz = nnz;
-        r->fo.assign(first_out, first_out + n + 1);
-        r->head.assign(head, head + nnz);
         for (uint64_t v = 0; v < n; ++v)
             if (first_out[v + 1] < first_out[v]) return KTRI_ERR_INVALID_CSR;
+        r->n = n;
+        r->nnz = nnz;
+        if (flags & KTRI_SUBMIT_BORROW) {
+            r->bfo = first_out;
+            r->bhead = head;
+        } else {
+            r->fo.assign(first_out, first_out + n + 1);
+            r->head.assign(head, head + nnz);
+            r->bfo = r->fo.data();
+            r->bhead = r->head.data();
+        }
     } else if (!graph_key) {
         return KTRI_ERR_INVALID_ARGUMENT;  // a repeat by key needs a key
     }

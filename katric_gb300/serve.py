@@ -33,21 +33,24 @@ class Server:
         self._mu = threading.Lock()
         self._sizes: dict[int, int] = {}  # key -> n of the graph last submitted under it
 
-    def submit(self, graph: Graph | None, key: int = 0, per_vertex: bool = True) -> int:
+    def submit(self, graph: Graph | None, key: int = 0, per_vertex: bool = True, borrow: bool = False) -> int:
+        """Queue a count.  borrow=True reads the graph's arrays in place: the Server keeps a
+        reference to the graph until wait() returns for this request."""
         rid = ctypes.c_uint64(0)
+        flags = (1 if per_vertex else 0) | (2 if borrow else 0)
         if graph is None:
             if not key:
                 raise ValueError("a repeat needs the key of a resident graph")
-            rc = self._L.ktri_server_submit(self._h, key, None, None, 0, 0, int(per_vertex), ctypes.byref(rid))
+            rc = self._L.ktri_server_submit(self._h, key, None, None, 0, 0, flags & 1, ctypes.byref(rid))
             n = self._sizes.get(key, 0)
         else:
             rc = self._L.ktri_server_submit(self._h, key, graph.first_out.ctypes.data,
                                             graph.head.ctypes.data if graph.nnz else None, graph.n, graph.nnz,
-                                            int(per_vertex), ctypes.byref(rid))
+                                            flags, ctypes.byref(rid))
             n = graph.n
         _native.check(rc)
         with self._mu:
-            self._meta[rid.value] = (n, per_vertex)
+            self._meta[rid.value] = (n, per_vertex, graph if borrow else None)
             if graph is not None and key:
                 self._sizes[key] = graph.n
         return rid.value
@@ -55,7 +58,7 @@ class Server:
     def wait(self, rid: int):
         """(total, per-vertex counts or None, latency in seconds)."""
         with self._mu:
-            n, want = self._meta.pop(rid)
+            n, want, _keep = self._meta.pop(rid)
         total = ctypes.c_uint64(0)
         lat = ctypes.c_double(0)
         pv = np.zeros(max(1, n), dtype=np.uint64) if want else None

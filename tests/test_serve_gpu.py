@@ -25,7 +25,7 @@ def test_results_alone_equal_results_in_the_mix():
 
         def client(lo, hi):
             for i in range(lo, hi):
-                rids[i] = srv.submit(graphs[i], key=1000 + i)
+                rids[i] = srv.submit(graphs[i], key=1000 + i, borrow=(i % 2 == 0))
 
         threads = [threading.Thread(target=client, args=(k * 23, min(len(graphs), (k + 1) * 23))) for k in range(4)]
         for t in threads:
