@@ -313,13 +313,46 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
 
 template <int BLOCK, int CAP, typename OffT>
 struct LargeLayout {
-    static constexpr int TS = 2 * CAP;  // table slots (at most half full)
+    static constexpr int TS = 2 * CAP;       // table slots (at most half full)
+    static constexpr int FWORDS = CAP / 2;   // filter words: 16 bits per key at CAP keys
+    static constexpr int WBUF = 64;          // per-warp buffer of filter survivors
     static constexpr size_t off_keys = 0;
-    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TS);
-    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * TS);
+    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TS);         // two u16 counters per word
+    static constexpr size_t off_filt = align16(off_hits + sizeof(u32) * (TS / 2));
+    static constexpr size_t off_wbuf = align16(off_filt + sizeof(u32) * FWORDS);
+    static constexpr size_t off_qy = align16(off_wbuf + sizeof(u32) * WBUF * (BLOCK / 32));
     static constexpr size_t off_qd = align16(off_qy + sizeof(u32) * LARGE_SEG);
     static constexpr size_t bytes = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
 };
+
+// Hit counters of the large owners' tables are 16-bit, two per word: a key gets at most one
+// hit per streamed list and a tile streams at most LARGE_SEG lists, so they cannot overflow.
+__device__ __forceinline__ void hit16(u32* hits32, u32 slot) { atomicAdd(&hits32[slot >> 1], 1u << ((slot & 1u) << 4)); }
+__device__ __forceinline__ u32 read16(const u32* hits32, u32 slot) { return (hits32[slot >> 1] >> ((slot & 1u) << 4)) & 0xFFFFu; }
+
+// Lookup with a 16-bit hit counter (same table layout as bucket_probe).
+__device__ __forceinline__ u32 bucket_probe16(const u32* keys, u32* hits32, u32 lg, u32 w) {
+    const u32 nb_mask = (1u << (lg - 2)) - 1;
+    u32 b = bucket_home(w, lg);
+    for (u32 it = 0; it <= nb_mask; ++it) {
+        const uint4 q = *reinterpret_cast<const uint4*>(keys + 4 * b);
+        const bool m0 = q.x == w, m1 = q.y == w, m2 = q.z == w, m3 = q.w == w;
+        if (m0 | m1 | m2 | m3) {
+            hit16(hits32, 4 * b + (m0 ? 0u : (m1 ? 1u : (m2 ? 2u : 3u))));
+            return 1u;
+        }
+        if (q.w == EMPTY_KEY) return 0u;
+        b = (b + 1) & nb_mask;
+    }
+    return 0u;
+}
+
+// One-hash membership filter of the owner's keys (2^fl bits): a clear bit is a sure miss.
+__device__ __forceinline__ u32 filter_bit(u32 w, u32 fl) { return (w * 0x85EBCA6Bu) >> (32 - fl); }
+__device__ __forceinline__ bool filter_test(const u32* filt, u32 fl, u32 w) {
+    const u32 h = filter_bit(w, fl);
+    return (filt[h >> 5] >> (h & 31u)) & 1u;
+}
 
 template <int BLOCK, int CAP, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
@@ -329,10 +362,11 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                                                        u64* __restrict__ partials, Control* ctl) {
     using L = LargeLayout<BLOCK, CAP, OffT>;
     constexpr int NW = BLOCK / 32;
-    constexpr int U = 8;  // loads in flight per lane when a warp streams a list
+    constexpr int U = 8;  // loads in flight per lane and list
     extern __shared__ __align__(16) unsigned char smem[];
     u32* keys = reinterpret_cast<u32*>(smem + L::off_keys);
     u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
+    u32* filt = reinterpret_cast<u32*>(smem + L::off_filt);
     u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
     Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
     __shared__ u64 s_red[NW];
@@ -341,6 +375,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
 
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32* wbuf = reinterpret_cast<u32*>(smem + L::off_wbuf) + warp * L::WBUF;
+    const u32 lt_mask = (1u << lane) - 1;
     const u64 ntiles = *(volatile unsigned long long*)&ctl->large_tiles;
     const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
     u64 local_total = 0;
@@ -361,14 +397,16 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         u64 T = 0;
         for (u32 c0 = 0; c0 < dx; c0 += CAP) {
             const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
-            u32 lg = ceil_log2(4 * klen);  // quarter full where the table has room
+            u32 lg = ceil_log2(4 * klen);  // a quarter full where the table has room
             if (lg > 31 - __clz((u32)L::TS)) lg = 31 - __clz((u32)L::TS);
             if (lg < 2) lg = 2;
-            const u32 size = 1u << lg;
-            for (u32 s = threadIdx.x; s < size; s += BLOCK) {
-                keys[s] = EMPTY_KEY;
-                hitc[s] = 0;
-            }
+            u32 fl = ceil_log2(16 * klen);  // filter bits: 16 per key
+            if (fl < 5) fl = 5;
+            if (fl > 31 - __clz((u32)(L::FWORDS * 32))) fl = 31 - __clz((u32)(L::FWORDS * 32));
+            const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
+            for (u32 s = threadIdx.x; s < size; s += BLOCK) keys[s] = EMPTY_KEY;
+            for (u32 s = threadIdx.x; s < size / 2; s += BLOCK) hitc[s] = 0;
+            for (u32 s = threadIdx.x; s < fwords; s += BLOCK) filt[s] = 0;
             if (threadIdx.x == 0) {
                 s_qn = 0;
                 s_next = 0;
@@ -377,6 +415,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
                 const u32 w = __ldg(headp + (u64)dxd.start + c0 + q);
                 if (!bucket_insert(keys, lg, w)) dup = 1;
+                const u32 h = filter_bit(w, fl);
+                atomicOr(&filt[h >> 5], 1u << (h & 31u));
             }
             __syncthreads();
             // scan the segment: short lists now, long lists into the queue
@@ -403,10 +443,11 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
 #pragma unroll
                             for (int c = 0; c < LONG_LIST / 4; ++c) {
                                 if (4 * c < (int)dy) {
-                                    hits += bucket_probe(keys, hitc, lg, qv[c].x);
-                                    if (4 * c + 1 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].y);
-                                    if (4 * c + 2 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].z);
-                                    if (4 * c + 3 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv[c].w);
+                                    const u32 wv[4] = {qv[c].x, qv[c].y, qv[c].z, qv[c].w};
+#pragma unroll
+                                    for (int k = 0; k < 4; ++k)
+                                        if (4 * c + k < (int)dy && filter_test(filt, fl, wv[k]))
+                                            hits += bucket_probe16(keys, hitc, lg, wv[k]);
                                 }
                             }
                             if (hits) {
@@ -423,13 +464,15 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
                 base = __shfl_sync(0xFFFFFFFFu, base, 0);
                 if (queue) {
-                    const u32 qi = base + __popc(ball & ((1u << lane) - 1));
+                    const u32 qi = base + __popc(ball & lt_mask);
                     qy[qi] = y;
                     qd[qi] = vy;
                 }
             }
             __syncthreads();
-            // long lists: one warp per list, taken from the queue one at a time
+            // long lists: one warp per list, taken from the queue.  Every entry is tested against
+            // the filter; the survivors are packed into the warp's buffer and looked up in the
+            // table 32 at a time, so the lookups run with full warps.
             const u32 qn = s_qn;
             while (true) {
                 u32 qi = 0;
@@ -438,7 +481,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 if (qi >= qn) break;
                 const Desc<OffT> vy = qd[qi];
                 const u32* lst = headp + (u64)vy.start;
-                u32 hits = 0;
+                u32 hits = 0, nbuf = 0;
                 for (u32 p0 = 0; p0 < vy.d; p0 += 32 * U) {
                     u32 w[U];
 #pragma unroll
@@ -447,9 +490,27 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                         w[u] = p < vy.d ? __ldg(lst + p) : EMPTY_KEY;
                     }
 #pragma unroll
-                    for (int u = 0; u < U; ++u)
-                        if (w[u] != EMPTY_KEY) hits += bucket_probe(keys, hitc, lg, w[u]);
+                    for (int u = 0; u < U; ++u) {
+                        if (p0 + 32 * u >= vy.d) break;
+                        const bool maybe = w[u] != EMPTY_KEY && filter_test(filt, fl, w[u]);
+                        const u32 ball = __ballot_sync(0xFFFFFFFFu, maybe);
+                        if (maybe) wbuf[nbuf + __popc(ball & lt_mask)] = w[u];
+                        nbuf += __popc(ball);
+                        if (nbuf >= 32) {
+                            __syncwarp();
+                            hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+                            const u32 rest = nbuf - 32;
+                            const u32 carry = lane < rest ? wbuf[32 + lane] : 0u;
+                            __syncwarp();
+                            if (lane < rest) wbuf[lane] = carry;
+                            __syncwarp();
+                            nbuf = rest;
+                        }
+                    }
                 }
+                __syncwarp();
+                if (lane < nbuf) hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+                __syncwarp();
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
                 if (lane == 0 && hits) {
                     atomicAdd(&cnt[qy[qi]], (u64)hits);
@@ -459,7 +520,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             __syncthreads();
             // flush the hits of every key
             for (u32 s = threadIdx.x; s < size; s += BLOCK) {
-                const u32 h = hitc[s];
+                const u32 h = read16(hitc, s);
                 if (h) atomicAdd(&cnt[keys[s]], (u64)h);
             }
             __syncthreads();
