@@ -81,8 +81,9 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     L.tile_i0 = take(sizeof(u32) * (ktri::base_tiles(n, nnz) + 2));
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
-        L.ltiles = take(sizeof(uint2) * ktri::large_tile_capacity(n, nnz, ktri::SMALL_D));
-        grid = (u32)(sms * 16);  // bound on small + large persistent grids (occupancy <= 8 each)
+        // medium-owner tiles, then large-owner tiles, each with room for every owner tile
+        L.ltiles = take(sizeof(uint2) * 2 * ktri::large_tile_capacity(n, nnz, ktri::SMALL_D));
+        grid = (u32)(sms * 48);  // bound on the small + medium + large persistent grids (occupancy <= 16 each)
     } else {
         L.mid = take(sizeof(u32) * (n + 1));
         L.big = take(sizeof(u32) * (n + 1));
@@ -193,9 +194,10 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
-    auto* ltiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
-    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, ltiles, autom ? (u32)ktri::SMALL_D : 0xFFFFFFFFu,
-                            ktri::LARGE_SEG, ctl, sms, st);
+    auto* mtiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
+    auto* ltiles = autom ? mtiles + ktri::large_tile_capacity(n, nnz, ktri::SMALL_D) : nullptr;
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? (u32)ktri::SMALL_D : 0xFFFFFFFFu,
+                            (u32)ktri::MEDIUM_D, ktri::LARGE_SEG, ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -207,11 +209,10 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl,
-                                                   sms, st, events ? ctx->ev[4] : nullptr,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, cnt,
+                                                   partials, ctl, sms, st, events ? ctx->ev[4] : nullptr,
                                                    events ? ctx->ev[5] : nullptr));
-        const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
-        ktri::launch_final(partials, np, d_total, ctl, st);
+        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
     } else {
         const int grid = ktri::count_grid_edges(sms);
         ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
@@ -343,18 +344,19 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
     auto* spanning = reinterpret_cast<u32*>(base + L.spanning);
     auto* partials = reinterpret_cast<u64*>(base + L.partials);
     auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
-    auto* ltiles = reinterpret_cast<uint2*>(base + L.ltiles);
+    auto* mtiles = reinterpret_cast<uint2*>(base + L.ltiles);
+    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, ktri::SMALL_D);
     // the control block (counters, error word) must start at zero; k_prep zeroes the
     // out-degrees and per-vertex counts; every other region is fully written before it is read
     if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return KTRI_ERR_CUDA;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
-    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, ltiles, (u32)ktri::SMALL_D, ktri::LARGE_SEG, ctl, sms, st);
-    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, ltiles, cnt, partials, ctl, sms, st,
-                                      nullptr, nullptr) != cudaSuccess)
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, (u32)ktri::SMALL_D, (u32)ktri::MEDIUM_D,
+                            ktri::LARGE_SEG, ctl, sms, st);
+    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, cnt, partials, ctl, sms,
+                                      st, nullptr, nullptr) != cudaSuccess)
         return KTRI_ERR_CUDA;
-    const u32 np = (u32)(ktri::count_grid_small<OffT>(sms) + ktri::count_grid_large<OffT>(sms));
-    ktri::launch_final(partials, np, d_total, ctl, st);
+    ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
     u32 herr = 0;
     if (cudaMemcpyAsync(&herr, &ctl->err, sizeof(u32), cudaMemcpyDeviceToHost, st) != cudaSuccess) return KTRI_ERR_CUDA;
@@ -714,10 +716,8 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
         return cuda_fail(ctx, e, "cudaMalloc(plan workspace)");
     }
     // occupancy queries happen once, outside the capture
-    (void)ktri::count_grid_small<u32>(ctx->num_sms);
-    (void)ktri::count_grid_large<u32>(ctx->num_sms);
-    (void)ktri::count_grid_small<u64>(ctx->num_sms);
-    (void)ktri::count_grid_large<u64>(ctx->num_sms);
+    (void)ktri::count_grid_auto<u32>(ctx->num_sms);
+    (void)ktri::count_grid_auto<u64>(ctx->num_sms);
     cudaStream_t cs = nullptr;
     cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     char* base = static_cast<char*>(p->ws);

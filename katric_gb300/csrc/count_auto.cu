@@ -354,6 +354,82 @@ __device__ __forceinline__ bool filter_test(const u32* filt, u32 fl, u32 w) {
     return (filt[h >> 5] >> (h & 31u)) & 1u;
 }
 
+// A whole warp streams one list (d entries at lst) through the owner's filter and table.
+// Entries that pass the filter are packed into the warp's buffer (64 entries) and looked up
+// 32 at a time.  Returns this lane's share of the hits.
+template <int U>
+__device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32 d, const u32* keys, u32* hitc, u32 lg,
+                                                const u32* filt, u32 fl, u32* wbuf, int lane, u32 lt_mask) {
+    u32 hits = 0, nbuf = 0;
+    for (u32 p0 = 0; p0 < d; p0 += 32 * U) {
+        u32 w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const u32 p = p0 + 32 * u + lane;
+            w[u] = p < d ? __ldg(lst + p) : EMPTY_KEY;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (p0 + 32 * u >= d) break;
+            const bool maybe = w[u] != EMPTY_KEY && filter_test(filt, fl, w[u]);
+            const u32 ball = __ballot_sync(0xFFFFFFFFu, maybe);
+            if (maybe) wbuf[nbuf + __popc(ball & lt_mask)] = w[u];
+            nbuf += __popc(ball);
+            if (nbuf >= 32) {
+                __syncwarp();
+                hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+                const u32 rest = nbuf - 32;
+                const u32 carry = lane < rest ? wbuf[32 + lane] : 0u;
+                __syncwarp();
+                if (lane < rest) wbuf[lane] = carry;
+                __syncwarp();
+                nbuf = rest;
+            }
+        }
+    }
+    __syncwarp();
+    if (lane < nbuf) hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+    __syncwarp();
+    return hits;
+}
+
+// A lane streams one short list (d <= LONG_LIST entries, 16-byte aligned) through the owner's
+// filter and table.
+template <typename OffT>
+__device__ __forceinline__ u32 lane_stream_short(const uint4* __restrict__ headp4, const Desc<OffT>& vy,
+                                                 const u32* keys, u32* hitc, u32 lg, const u32* filt, u32 fl) {
+    const u32 dy = vy.d;
+    const u64 q0 = (u64)vy.start >> 2;
+    uint4 qv[LONG_LIST / 4];
+#pragma unroll
+    for (int c = 0; c < LONG_LIST / 4; ++c)
+        qv[c] = 4 * c < (int)dy ? __ldg(headp4 + q0 + c) : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+    u32 hits = 0;
+#pragma unroll
+    for (int c = 0; c < LONG_LIST / 4; ++c) {
+        if (4 * c < (int)dy) {
+            const u32 wv[4] = {qv[c].x, qv[c].y, qv[c].z, qv[c].w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (4 * c + k < (int)dy && filter_test(filt, fl, wv[k])) hits += bucket_probe16(keys, hitc, lg, wv[k]);
+        }
+    }
+    return hits;
+}
+
+// Table and filter sizes of an owner chunk of klen keys: a quarter-full table (at most
+// max_lg) and 16 filter bits per key (at most max_fl).
+__device__ __forceinline__ void chunk_sizes(u32 klen, u32 max_lg, u32 max_fl, u32* lg, u32* fl) {
+    u32 a = ceil_log2(4 * klen);
+    if (a > max_lg) a = max_lg;
+    if (a < 2) a = 2;
+    u32 f = ceil_log2(16 * klen);
+    if (f > max_fl) f = max_fl;
+    if (f < 5) f = 5;
+    *lg = a;
+    *fl = f;
+}
+
 template <int BLOCK, int CAP, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, const Desc<OffT>* __restrict__ vdesc,
@@ -397,12 +473,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         u64 T = 0;
         for (u32 c0 = 0; c0 < dx; c0 += CAP) {
             const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
-            u32 lg = ceil_log2(4 * klen);  // a quarter full where the table has room
-            if (lg > 31 - __clz((u32)L::TS)) lg = 31 - __clz((u32)L::TS);
-            if (lg < 2) lg = 2;
-            u32 fl = ceil_log2(16 * klen);  // filter bits: 16 per key
-            if (fl < 5) fl = 5;
-            if (fl > 31 - __clz((u32)(L::FWORDS * 32))) fl = 31 - __clz((u32)(L::FWORDS * 32));
+            u32 lg, fl;
+            chunk_sizes(klen, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FWORDS * 32)), &lg, &fl);
             const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
             for (u32 s = threadIdx.x; s < size; s += BLOCK) keys[s] = EMPTY_KEY;
             for (u32 s = threadIdx.x; s < size / 2; s += BLOCK) hitc[s] = 0;
@@ -433,23 +505,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                     const u32 dy = vy.d;
                     if (dy > 0 && key_less(dy, y, dx, x)) {
                         if (dy <= (u32)LONG_LIST) {
-                            const u64 q0 = (u64)vy.start >> 2;
-                            uint4 qv[LONG_LIST / 4];
-#pragma unroll
-                            for (int c = 0; c < LONG_LIST / 4; ++c)
-                                qv[c] = 4 * c < (int)dy ? __ldg(headp4 + q0 + c)
-                                                        : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
-                            u32 hits = 0;
-#pragma unroll
-                            for (int c = 0; c < LONG_LIST / 4; ++c) {
-                                if (4 * c < (int)dy) {
-                                    const u32 wv[4] = {qv[c].x, qv[c].y, qv[c].z, qv[c].w};
-#pragma unroll
-                                    for (int k = 0; k < 4; ++k)
-                                        if (4 * c + k < (int)dy && filter_test(filt, fl, wv[k]))
-                                            hits += bucket_probe16(keys, hitc, lg, wv[k]);
-                                }
-                            }
+                            const u32 hits = lane_stream_short<OffT>(headp4, vy, keys, hitc, lg, filt, fl);
                             if (hits) {
                                 atomicAdd(&cnt[y], (u64)hits);
                                 T += hits;
@@ -480,37 +536,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 qi = __shfl_sync(0xFFFFFFFFu, qi, 0);
                 if (qi >= qn) break;
                 const Desc<OffT> vy = qd[qi];
-                const u32* lst = headp + (u64)vy.start;
-                u32 hits = 0, nbuf = 0;
-                for (u32 p0 = 0; p0 < vy.d; p0 += 32 * U) {
-                    u32 w[U];
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const u32 p = p0 + 32 * u + lane;
-                        w[u] = p < vy.d ? __ldg(lst + p) : EMPTY_KEY;
-                    }
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        if (p0 + 32 * u >= vy.d) break;
-                        const bool maybe = w[u] != EMPTY_KEY && filter_test(filt, fl, w[u]);
-                        const u32 ball = __ballot_sync(0xFFFFFFFFu, maybe);
-                        if (maybe) wbuf[nbuf + __popc(ball & lt_mask)] = w[u];
-                        nbuf += __popc(ball);
-                        if (nbuf >= 32) {
-                            __syncwarp();
-                            hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
-                            const u32 rest = nbuf - 32;
-                            const u32 carry = lane < rest ? wbuf[32 + lane] : 0u;
-                            __syncwarp();
-                            if (lane < rest) wbuf[lane] = carry;
-                            __syncwarp();
-                            nbuf = rest;
-                        }
-                    }
-                }
-                __syncwarp();
-                if (lane < nbuf) hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
-                __syncwarp();
+                u32 hits = warp_stream_list<U>(headp + (u64)vy.start, vy.d, keys, hitc, lg, filt, fl, wbuf, lane,
+                                               lt_mask);
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
                 if (lane == 0 && hits) {
                     atomicAdd(&cnt[qy[qi]], (u64)hits);
@@ -533,6 +560,122 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
     if (threadIdx.x == 0) partials[blockIdx.x] = local_total;
+}
+
+// Medium owners (small threshold < out-degree <= MEDIUM_D): one warp per (owner, segment)
+// tile, with its own table, filter and buffer in shared memory, so a tile needs no block
+// barrier.  Most owner tiles of skewed graphs are of this kind and carry little work each.
+template <int BLOCK>
+struct MediumLayout {
+    static constexpr int NW = BLOCK / 32;
+    static constexpr int TS = 4 * MEDIUM_D;  // table slots per warp (at most a quarter full)
+    static constexpr int FW = MEDIUM_D / 2;  // filter words per warp (16 bits per key)
+    static constexpr int WBUF = 64;
+    static constexpr int PER_WARP = TS + TS / 2 + FW + WBUF;  // u32 words: keys, 16-bit hits, filter, buffer
+    static constexpr size_t bytes = sizeof(u32) * PER_WARP * NW;
+};
+
+template <int BLOCK, typename OffT>
+__global__ void __launch_bounds__(BLOCK)
+    k_count_medium(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
+                   const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp,
+                   const uint2* __restrict__ mtiles, u64* __restrict__ cnt, u64* __restrict__ partials,
+                   Control* ctl) {
+    using L = MediumLayout<BLOCK>;
+    constexpr int U = 8;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ u64 s_red[L::NW];
+    if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32* keys = reinterpret_cast<u32*>(smem) + warp * L::PER_WARP;
+    u32* hitc = keys + L::TS;
+    u32* filt = hitc + L::TS / 2;
+    u32* wbuf = filt + L::FW;
+    const u32 lt_mask = (1u << lane) - 1;
+    const u64 ntiles = *(volatile unsigned long long*)&ctl->medium_tiles;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    u64 local_total = 0;
+    u32 dup = 0;
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->medium_next, 1ull);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        if (t >= ntiles) break;
+        const uint2 tl = mtiles[t];
+        const u64 x = tl.x;
+        const Desc<OffT> dxd = load_desc(vdesc + x);
+        const u32 dx = dxd.d;
+        const u64 fx1 = fo[x + 1];
+        const u64 a = fo[x] + (u64)tl.y * LARGE_SEG;
+        const u64 b = a + LARGE_SEG < fx1 ? a + LARGE_SEG : fx1;
+        u32 lg, fl;
+        chunk_sizes(dx, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FW * 32)), &lg, &fl);
+        const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
+        for (u32 i = lane; i < size; i += 32) keys[i] = EMPTY_KEY;
+        for (u32 i = lane; i < size / 2; i += 32) hitc[i] = 0;
+        for (u32 i = lane; i < fwords; i += 32) filt[i] = 0;
+        __syncwarp();
+        for (u32 q = lane; q < dx; q += 32) {
+            const u32 w = __ldg(headp + (u64)dxd.start + q);
+            if (!bucket_insert(keys, lg, w)) dup = 1;
+            const u32 h = filter_bit(w, fl);
+            atomicOr(&filt[h >> 5], 1u << (h & 31u));
+        }
+        __syncwarp();
+        u32 T = 0;
+        for (u64 e0 = a; e0 < b; e0 += 32) {
+            const u64 e = e0 + lane;
+            u32 y = 0;
+            Desc<OffT> vy;
+            vy.start = 0;
+            vy.d = 0;
+            bool longl = false;
+            if (e < b) {
+                y = __ldg(head + e);
+                vy = load_desc(vdesc + y);
+                const u32 dy = vy.d;
+                if (dy > 0 && key_less(dy, y, dx, x)) {
+                    if (dy <= (u32)LONG_LIST) {
+                        const u32 hits = lane_stream_short<OffT>(headp4, vy, keys, hitc, lg, filt, fl);
+                        if (hits) {
+                            atomicAdd(&cnt[y], (u64)hits);
+                            T += hits;
+                        }
+                    } else {
+                        longl = true;
+                    }
+                }
+            }
+            u32 ball = __ballot_sync(0xFFFFFFFFu, longl);
+            while (ball) {  // the warp streams this chunk's long lists one at a time
+                const int src = __ffs(ball) - 1;
+                ball &= ball - 1;
+                const u32 yy = __shfl_sync(0xFFFFFFFFu, y, src);
+                const u64 ys = (u64)__shfl_sync(0xFFFFFFFFu, (unsigned long long)vy.start, src);
+                const u32 yd = __shfl_sync(0xFFFFFFFFu, vy.d, src);
+                u32 hits = warp_stream_list<U>(headp + ys, yd, keys, hitc, lg, filt, fl, wbuf, lane, lt_mask);
+                hits = __reduce_add_sync(0xFFFFFFFFu, hits);
+                if (lane == 0 && hits) {
+                    atomicAdd(&cnt[yy], (u64)hits);
+                    T += hits;
+                }
+            }
+        }
+        __syncwarp();
+        for (u32 i = lane; i < size; i += 32) {
+            const u32 h = read16(hitc, i);
+            if (h) atomicAdd(&cnt[keys[i]], (u64)h);
+        }
+        const u32 wt = __reduce_add_sync(0xFFFFFFFFu, T);
+        if (lane == 0 && wt) {
+            atomicAdd(&cnt[x], (u64)wt);
+            local_total += wt;
+        }
+        __syncwarp();
+    }
+    if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+    const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = bt;
 }
 
 // Sum of the per-block partial totals (a u64 tree reduction in one block).
@@ -612,6 +755,7 @@ template <typename OffT>
 using SmallL = SmallLayout<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>;
 template <typename OffT>
 using LargeL = LargeLayout<LARGE_BLOCK, LARGE_CAP, OffT>;
+using MediumL = MediumLayout<MEDIUM_BLOCK>;
 
 template <typename OffT>
 int occupancy_small() {
@@ -621,6 +765,18 @@ int occupancy_small() {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<OffT>::bytes);
         int o = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<OffT>::bytes);
+        occ = o > 0 ? o : 1;
+    }
+    return occ;
+}
+template <typename OffT>
+int occupancy_medium() {
+    static int occ = -1;
+    if (occ < 0) {
+        auto kern = k_count_medium<MEDIUM_BLOCK, OffT>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MediumL::bytes);
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, MEDIUM_BLOCK, MediumL::bytes);
         occ = o > 0 ? o : 1;
     }
     return occ;
@@ -644,23 +800,34 @@ int count_grid_small(int num_sms) {
     return num_sms * occupancy_small<OffT>();
 }
 template <typename OffT>
+int count_grid_medium(int num_sms) {
+    return num_sms * occupancy_medium<OffT>();
+}
+template <typename OffT>
 int count_grid_large(int num_sms) {
     return num_sms * occupancy_large<OffT>();
+}
+template <typename OffT>
+int count_grid_auto(int num_sms) {
+    return count_grid_small<OffT>(num_sms) + count_grid_medium<OffT>(num_sms) + count_grid_large<OffT>(num_sms);
 }
 
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl,
-                              int num_sms,
-                              cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large) {
+                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u64* cnt, u64* partials,
+                              Control* ctl, int num_sms, cudaStream_t st, cudaEvent_t after_small,
+                              cudaEvent_t after_large) {
     const int gs = count_grid_small<OffT>(num_sms);
+    const int gm = count_grid_medium<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
     k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
         <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, cnt, partials, ctl);
     if (after_small) cudaEventRecord(after_small, st);
+    k_count_medium<MEDIUM_BLOCK, OffT>
+        <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, cnt, partials + gs, ctl);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
-        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs, ctl);
+        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs + gm, ctl);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
 }
@@ -688,11 +855,15 @@ template int count_grid_small<u32>(int);
 template int count_grid_small<u64>(int);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
+template int count_grid_medium<u32>(int);
+template int count_grid_medium<u64>(int);
+template int count_grid_auto<u32>(int);
+template int count_grid_auto<u64>(int);
 template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*,
+                                            const uint2*, const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*,
+                                            const uint2*, const uint2*,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
 template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);

@@ -49,7 +49,9 @@ struct Control {
     unsigned long long stat_oriented;    // collect_stats: sum of out-degrees
     unsigned long long sort_mid;         // lists sorted by whole blocks in shared memory
     unsigned long long sort_big;         // lists sorted by whole blocks in global scratch
-    unsigned long long pad[4];
+    unsigned long long medium_tiles;     // number of (owner, segment) tiles for medium owners
+    unsigned long long medium_next;      // dynamic tile cursor of the medium-owner kernel
+    unsigned long long pad[2];
 };
 
 }  // namespace ktri

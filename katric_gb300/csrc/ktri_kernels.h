@@ -17,6 +17,8 @@ constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
 constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
+constexpr int MEDIUM_D = 256;        // out-degree bound of the warp-per-tile kernel's owners
+constexpr int MEDIUM_BLOCK = 256;
 constexpr int LARGE_BLOCK = 256;
 constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of the vertex kernel
 constexpr u32 LARGE_SEG = 1024;      // adjacency slots per (owner, segment) tile
@@ -39,19 +41,25 @@ void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, 
                  int num_sms, cudaStream_t st);
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
                    u32* dplus, u32* spanning, Control* ctl, cudaStream_t st);
+// Owner tiles: medium owners' tiles are written to mtiles, large owners' to ltiles (each
+// array holds large_tile_capacity entries).
 template <typename OffT>
-void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
-                 Control* ctl, int num_sms, cudaStream_t st);
+void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
+                 u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st);
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
 int count_grid_small(int num_sms);
 template <typename OffT>
+int count_grid_medium(int num_sms);
+template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
+int count_grid_auto(int num_sms);  // small + medium + large
+template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* ltiles, u64* cnt, u64* partials, Control* ctl,
-                              int num_sms,
+                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u64* cnt, u64* partials,
+                              Control* ctl, int num_sms,
                               cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
 void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs, u64 n, u64* totals, Control* ctl,

@@ -206,14 +206,15 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
 // out-degree threshold.
 template <typename OffT>
 __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict__ dplus, Desc<OffT>* __restrict__ vdesc,
-                       uint2* __restrict__ ltiles, u32 small_d, u32 seg, Control* ctl) {
+                       uint2* __restrict__ mtiles, uint2* __restrict__ ltiles, u32 small_d, u32 medium_d, u32 seg,
+                       Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
     const u64 warp_global = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
     for (u64 base = warp_global * 32; base < n; base += nwarps * 32) {
         const u64 v = base + lane;
-        u32 nt = 0;
+        u32 nm = 0, nl = 0;
         if (v < n) {
             const u64 a = fo[v], b = fo[v + 1];
             const u32 d = dplus[v];
@@ -222,21 +223,28 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
             ds.d = d;
             if constexpr (sizeof(OffT) == 8) ds.pad = 0;
             vdesc[v] = ds;
-            if (d > small_d) nt = (u32)((b - a + seg - 1) / seg);
+            const u32 nt = d > small_d ? (u32)((b - a + seg - 1) / seg) : 0u;
+            if (d > medium_d) nl = nt;
+            else nm = nt;
         }
-        // warp-aggregated reservation of tile slots
-        u32 incl = nt;
+        // warp-aggregated reservation of tile slots, one list per owner class
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += y;
+        for (int cls = 0; cls < 2; ++cls) {
+            const u32 mine = cls == 0 ? nm : nl;
+            u32 incl = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const u32 wsum = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            u64 wbase = 0;
+            if (lane == 31 && wsum) wbase = atomicAdd(cls == 0 ? &ctl->medium_tiles : &ctl->large_tiles, (u64)wsum);
+            wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+            const u64 my = wbase + incl - mine;
+            uint2* out = cls == 0 ? mtiles : ltiles;
+            for (u32 s = 0; s < mine; ++s) out[my + s] = make_uint2((u32)v, s);
         }
-        const u32 wsum = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        u64 wbase = 0;
-        if (lane == 31 && wsum) wbase = atomicAdd(&ctl->large_tiles, (u64)wsum);
-        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
-        const u64 my = wbase + incl - nt;
-        for (u32 s = 0; s < nt; ++s) ltiles[my + s] = make_uint2((u32)v, s);
     }
 }
 
@@ -261,16 +269,18 @@ void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* de
 }
 
 template <typename OffT>
-void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* ltiles, u32 small_d, u32 seg,
-                 Control* ctl, int num_sms, cudaStream_t st) {
+void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
+                 u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u64 blocks = (n + 255) / 256;
     u64 cap = (u64)num_sms * 8;
     k_desc<OffT><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(
-        fo, n, dplus, reinterpret_cast<Desc<OffT>*>(vdesc), ltiles, small_d, seg, ctl);
+        fo, n, dplus, reinterpret_cast<Desc<OffT>*>(vdesc), mtiles, ltiles, small_d, medium_d, seg, ctl);
 }
 
-template void launch_desc<u32>(const u64*, u64, const u32*, void*, uint2*, u32, u32, Control*, int, cudaStream_t);
-template void launch_desc<u64>(const u64*, u64, const u32*, void*, uint2*, u32, u32, Control*, int, cudaStream_t);
+template void launch_desc<u32>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, Control*, int,
+                               cudaStream_t);
+template void launch_desc<u64>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, Control*, int,
+                               cudaStream_t);
 
 }  // namespace ktri
