@@ -186,6 +186,14 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def tune_cache_path() -> str:
+    """Persisted autotuner choices: $KTRI_TUNE_CACHE, else ~/.cache/katric_gb300/tune.jsonl."""
+    path = os.environ.get("KTRI_TUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "katric_gb300",
+                                                              "tune.jsonl")
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    return path
+
+
 def run_batch(args):
     """Batched workload: one captured plan (CUDA graph) over the packed union of all graphs,
     against the plain loop of one device entry-point call per graph, both timed here."""
@@ -204,8 +212,18 @@ def run_batch(args):
     tot = torch.zeros(k, dtype=torch.int64, device=dev)
     pv = torch.zeros(n, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream(dev)
+    # bins, segment and strategy from the autotuner, tuned on a prefix of the batch (about an
+    # eighth of the graphs) and persisted; later runs of the same shape class read the choice back
+    ks = max(1, min(k, k // 8))
+    ns = int(b.graph_first[ks])
+    t0 = time.perf_counter()
+    conf, tune = ctr.autotune(fo.data_ptr(), hd.data_ptr(), ns, int(b.union.first_out[ns]), gf.data_ptr(), ks,
+                              cache_path=tune_cache_path(), stream=stream.cuda_stream)
+    tune.update({"sample_graphs": ks, "tune_s": round(time.perf_counter() - t0, 2),
+                 "chosen": {"intersection_method": conf.intersection_method, "small_outdegree": conf.small_outdegree,
+                            "medium_outdegree": conf.medium_outdegree, "segment": conf.segment}})
     plan = ctr.plan_batch(fo.data_ptr(), hd.data_ptr(), n, nnz, gf.data_ptr(), k, tot.data_ptr(), pv.data_ptr(),
-                          Config())
+                          conf)
     for _ in range(args.warmup):
         plan.launch(stream.cuda_stream)
     plan.check()
@@ -234,7 +252,7 @@ def run_batch(args):
         per.append((f.contiguous(), h.contiguous(), int(e - a), int(ufo[e] - ufo[a])))
     out_t = torch.zeros(k, dtype=torch.int64, device=dev)
     out_pv = torch.zeros(int(max(p[2] for p in per)) + 1, dtype=torch.int64, device=dev)
-    cfg = Config()
+    cfg = conf
 
     def plain_pass():
         for g, (f, h, gn, gnnz) in enumerate(per):
@@ -260,6 +278,7 @@ def run_batch(args):
         "plain_loop": {"ms": plain_ms, "graphs_per_s": k / (plain_ms / 1e3), "edges_per_s": b.union.m / (plain_ms / 1e3),
                        "path": "ktri_count_csr_device per graph, one stream, device-resident inputs"},
         "batched_vs_plain": plain_ms / ms,
+        "autotune": tune,
         "triangles_total": int(ref_tot.sum().item()),
         "gpu_launches": 9 * args.steps,
         "clocks": clk,

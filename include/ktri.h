@@ -50,13 +50,18 @@ extern "C" {
 typedef struct ktri_opts {
     uint32_t struct_size;          /* sizeof(ktri_opts); 0 is read as "all defaults" */
     int32_t intersection_method;   /* KTRI_METHOD_* */
-    uint32_t small_outdegree;      /* owners with out-degree <= this use the tile kernel (0 = tuned default) */
+    uint32_t small_outdegree;      /* owners with out-degree <= this use the tile kernel: 1..32 (0 = default 32) */
     uint32_t collect_stats;        /* 1: also compute wedge_checks / intersection work counters */
     uint64_t binary_intersection_cutoff; /* Config::binary_intersection_cutoff (config.h:173), default 1000 */
     double hybrid_cutoff_scale;    /* Config::hybrid_cutoff_scale (config.h:174), default 1.0 */
     uint32_t force_wide_offsets;   /* 1: 64-bit out-list offsets even where 32 bits suffice (the path
                                       graphs with nnz + 3n > 2^32 take; exposed for testing) */
-    uint32_t reserved[7];
+    uint32_t medium_outdegree;     /* owners above small_outdegree and at most this use the warp-per-tile
+                                      kernel, larger ones the block-per-tile kernel: small_outdegree..256
+                                      (0 = default 256) */
+    uint32_t segment;              /* adjacency slots per owner tile of those two kernels: a power of two
+                                      in 64..1024 (0 = default 1024) */
+    uint32_t reserved[5];
 } ktri_opts;
 
 /* Counters of the last run on a context, named after the reference's Statistics fields
@@ -166,6 +171,45 @@ int ktri_plan_launch(ktri_plan* plan, void* stream);
 int ktri_plan_check(ktri_plan* plan);
 int ktri_plan_destroy(ktri_plan* plan);
 
+/* ---- oriented lists: the katric local phase -----------------------------------------------
+ * Replaces CetricEdgeIterator::run_local on one rank's graph (cetric_edge_iterator.h:173-227,
+ * called from cetric.h:431,450 and :827,847), which walks lists the caller has already
+ * oriented: out_adj of the local vertices and, in the variant with ghosts (:301-388), ghost_adj
+ * of the ghosts.  Give every vertex (local and ghost, numbered 0..n-1) its list; m is the total
+ * length.  The count is that of the triangles whose three edges appear in the lists, which is
+ * what run_local finds, whatever orientation the caller used.  Every edge must appear in exactly
+ * one of its endpoints' lists; lists may be in any order.  Out-of-range ids and self-loops are
+ * reported as KTRI_ERR_INVALID_CSR; an edge listed at both endpoints is reported as a duplicate
+ * where a shared-memory table meets it (not guaranteed).  Per-vertex counts are indexed like
+ * the lists (ghosts included). */
+int ktri_count_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t m,
+                       uint64_t* total_out, uint64_t* per_vertex_out, const ktri_opts* opts);
+int ktri_count_dag_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t m,
+                          uint64_t* d_total, uint64_t* d_per_vertex, const ktri_opts* opts, void* stream);
+
+/* ---- autotuning ---------------------------------------------------------------------------
+ * No counterpart in the reference (its strategy is a command-line choice, --intersection-method,
+ * apps/parse_parameters.h:156-158).  ktri_autotune times candidate configurations of one count
+ * of the given device input (one graph when d_graph_first is NULL, else a packed batch):
+ * intersection strategy, small_outdegree, medium_outdegree and segment, and writes the fastest
+ * into *opts (other fields are kept).  With a cache_path the choice is looked up first and, when
+ * timed, appended as one JSON line keyed by the input's shape class (compute capability, SM
+ * count, floor log2 of graphs, n, nnz and the largest degree).  The call synchronises `stream`. */
+typedef struct ktri_tuning {
+    uint32_t struct_size;
+    int32_t intersection_method; /* the chosen configuration */
+    uint32_t small_outdegree, medium_outdegree, segment;
+    uint32_t from_cache;         /* 1: read from the cache file, nothing timed */
+    uint32_t candidates;         /* configurations timed */
+    uint32_t reserved0;
+    double ms;                   /* device time of one count with the chosen configuration */
+    double default_ms;           /* the same with the library defaults (0 when read from the cache) */
+    char signature[96];          /* the shape class */
+} ktri_tuning;
+int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t nnz,
+                  const uint64_t* d_graph_first, uint64_t num_graphs, const char* cache_path, ktri_opts* opts,
+                  ktri_tuning* out, void* stream);
+
 /* ---- serving ------------------------------------------------------------------------------
  * No counterpart in the reference.  A request loop with continuous batching: requests (one
  * graph each) queue up; a worker thread packs the waiting ones into a batch under the device
@@ -174,8 +218,10 @@ int ktri_plan_destroy(ktri_plan* plan);
  * device, keyed by graph_key) until the budget needs their room; a request for a resident
  * key is answered from the resident counts.  submit copies the caller's CSR, or with
  * KTRI_SUBMIT_BORROW reads it in place (the caller keeps it alive and unchanged until wait
- * returns); first_out may be NULL to repeat a resident key.  wait blocks until the request is
- * done and reports its latency (submit to completion). */
+ * returns); first_out may be NULL to repeat a key that is resident, queued or counting.  A
+ * request whose key is queued or counting (same n and nnz) joins that count instead of
+ * starting another.  wait blocks until the request is done and reports its latency (submit to
+ * completion). */
 #define KTRI_SUBMIT_PER_VERTEX 1u /* return per-vertex counts */
 #define KTRI_SUBMIT_BORROW 2u     /* read the caller's CSR in place instead of copying it */
 typedef struct ktri_server ktri_server;
@@ -190,7 +236,8 @@ typedef struct ktri_server_opts {
 typedef struct ktri_server_stats {
     uint64_t submitted, completed, batches, batched_graphs, cache_hits, evictions, resident_graphs, resident_bytes,
         peak_inflight_batches;
-    uint64_t reserved[7];
+    uint64_t coalesced; /* requests answered by the count of an earlier queued request with their key */
+    uint64_t reserved[6];
 } ktri_server_stats;
 int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out);
 int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,

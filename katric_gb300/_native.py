@@ -48,7 +48,9 @@ class Opts(ctypes.Structure):
         ("binary_intersection_cutoff", ctypes.c_uint64),
         ("hybrid_cutoff_scale", ctypes.c_double),
         ("force_wide_offsets", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 7),
+        ("medium_outdegree", ctypes.c_uint32),
+        ("segment", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 5),
     ]
 
 
@@ -66,7 +68,23 @@ class ServerOpts(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "batches", "batched_graphs", "cache_hits",
                                               "evictions", "resident_graphs", "resident_bytes",
-                                              "peak_inflight_batches")] + [("reserved", ctypes.c_uint64 * 7)]
+                                              "peak_inflight_batches", "coalesced")] + [("reserved", ctypes.c_uint64 * 6)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("intersection_method", ctypes.c_int32),
+        ("small_outdegree", ctypes.c_uint32),
+        ("medium_outdegree", ctypes.c_uint32),
+        ("segment", ctypes.c_uint32),
+        ("from_cache", ctypes.c_uint32),
+        ("candidates", ctypes.c_uint32),
+        ("reserved0", ctypes.c_uint32),
+        ("ms", ctypes.c_double),
+        ("default_ms", ctypes.c_double),
+        ("signature", ctypes.c_char * 96),
+    ]
 
 
 class RunStats(ctypes.Structure):
@@ -112,6 +130,9 @@ SIGNATURES = {
     "ktri_plan_launch": (ctypes.c_int, [P, P]),
     "ktri_plan_check": (ctypes.c_int, [P]),
     "ktri_plan_destroy": (ctypes.c_int, [P]),
+    "ktri_count_dag_ctx": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts)]),
+    "ktri_count_dag_device": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts), P]),
+    "ktri_autotune": (ctypes.c_int, [P, P, P, U64, U64, P, U64, CP, ctypes.POINTER(Opts), ctypes.POINTER(Tuning), P]),
     "ktri_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServerOpts), PP]),
     "ktri_server_submit": (ctypes.c_int, [P, U64, P, P, U64, U64, U32, ctypes.POINTER(U64)]),
     "ktri_server_wait": (ctypes.c_int, [P, U64, ctypes.POINTER(U64), P, ctypes.POINTER(ctypes.c_double)]),

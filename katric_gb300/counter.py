@@ -54,6 +54,9 @@ class Config:
     collect_stats: bool = False
     device: int = 0
     force_wide_offsets: bool = False
+    small_outdegree: int = 0    # owner bins of the "auto" kernels (0 = library default; see ktri_opts)
+    medium_outdegree: int = 0
+    segment: int = 0
 
     def opts(self) -> _native.Opts:
         o = _native.Opts()
@@ -62,7 +65,9 @@ class Config:
             o.intersection_method = METHOD_BY_NAME[self.intersection_method.lower()]
         except KeyError:
             raise ValueError(f"unknown intersection method {self.intersection_method!r}") from None
-        o.small_outdegree = 0
+        o.small_outdegree = self.small_outdegree
+        o.medium_outdegree = self.medium_outdegree
+        o.segment = self.segment
         o.collect_stats = 1 if self.collect_stats else 0
         o.binary_intersection_cutoff = self.binary_intersection_cutoff
         o.hybrid_cutoff_scale = self.hybrid_cutoff_scale
@@ -153,6 +158,29 @@ class TriangleCounter:
         self._check(self._L.ktri_count_csr_device(self._ctx, first_out_ptr, head_ptr, n, nnz, total_ptr,
                                                   per_vertex_ptr, ctypes.byref(opts), stream or None))
 
+    def count_dag(self, first_out, head, conf: Config | None = None, per_vertex: bool = True):
+        """CetricEdgeIterator::run_local on lists the caller oriented (out_adj of local vertices,
+        ghost_adj of ghosts): the triangles whose three edges appear in the lists.
+        Returns (total, per-vertex counts or None)."""
+        conf = conf or Config()
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, m = len(fo) - 1, len(hd)
+        total = ctypes.c_uint64(0)
+        pv = np.zeros(max(n, 1), dtype=np.uint64) if per_vertex else None
+        opts = conf.opts()
+        self._check(self._L.ktri_count_dag_ctx(self._ctx, fo.ctypes.data, hd.ctypes.data if m else None, n, m,
+                                               ctypes.byref(total), pv.ctypes.data if pv is not None else None,
+                                               ctypes.byref(opts)))
+        return int(total.value), (pv[:n] if pv is not None else None)
+
+    def count_dag_device(self, first_out_ptr: int, head_ptr: int, n: int, m: int, total_ptr: int,
+                         per_vertex_ptr: int | None = None, conf: Config | None = None, stream: int = 0) -> None:
+        conf = conf or Config()
+        opts = conf.opts()
+        self._check(self._L.ktri_count_dag_device(self._ctx, first_out_ptr, head_ptr, n, m, total_ptr,
+                                                  per_vertex_ptr, ctypes.byref(opts), stream or None))
+
     def check(self) -> None:
         self._check(self._L.ktri_ctx_check(self._ctx))
 
@@ -194,6 +222,28 @@ class TriangleCounter:
                                                    graph_first_ptr, num_graphs, totals_ptr, per_vertex_ptr,
                                                    ctypes.byref(opts), ctypes.byref(h)))
         return Plan(self, h)
+
+    def autotune(self, first_out_ptr: int, head_ptr: int, n: int, nnz: int, graph_first_ptr: int | None = None,
+                 num_graphs: int = 0, cache_path: str | None = None, conf: Config | None = None,
+                 stream: int = 0) -> tuple[Config, dict]:
+        """Time candidate configurations of one count of this device input (a packed batch when
+        graph_first_ptr is given) and return (conf with the fastest strategy, owner bins and
+        segment, details).  With cache_path the choice is read from / appended to that JSON-lines
+        file, keyed by the input's shape class."""
+        conf = conf or Config()
+        opts = conf.opts()
+        res = _native.Tuning()
+        res.struct_size = ctypes.sizeof(_native.Tuning)
+        path = cache_path.encode() if cache_path else None
+        self._check(self._L.ktri_autotune(self._ctx, first_out_ptr, head_ptr, n, nnz, graph_first_ptr,
+                                          num_graphs if graph_first_ptr else 0, path, ctypes.byref(opts),
+                                          ctypes.byref(res), stream or None))
+        name = {v: k for k, v in METHOD_BY_NAME.items() if "_" not in k}[res.intersection_method]
+        tuned = dataclasses.replace(conf, intersection_method=name, small_outdegree=res.small_outdegree,
+                                    medium_outdegree=res.medium_outdegree, segment=res.segment)
+        info = {"from_cache": bool(res.from_cache), "candidates": int(res.candidates), "ms": float(res.ms),
+                "default_ms": float(res.default_ms), "signature": res.signature.decode()}
+        return tuned, info
 
     def orient(self, first_out, head):
         """Oriented, id-sorted out-lists as a compact CSR (u64 offsets, u32 ids)."""

@@ -61,7 +61,7 @@ u64 isqrt_ceil(u64 x) {
 
 // Workspace of one count.  num_sms = 0 sizes the grids for the largest supported part.
 Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs, bool internal_cnt,
-                   bool force_wide = false) {
+                   bool force_wide = false, u32 small_d = (u32)ktri::SMALL_D, u32 seg = ktri::LARGE_SEG) {
     Layout L;
     const u64 cap = ktri::oriented_capacity(n, nnz);
     L.wide = force_wide || cap > 0xFFFFFFFFull;
@@ -82,7 +82,7 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
         // medium-owner tiles, then large-owner tiles, each with room for every owner tile
-        L.ltiles = take(sizeof(uint2) * 2 * ktri::large_tile_capacity(n, nnz, ktri::SMALL_D));
+        L.ltiles = take(sizeof(uint2) * 2 * ktri::large_tile_capacity(n, nnz, small_d, seg));
         grid = (u32)(sms * 48);  // bound on the small + medium + large persistent grids (occupancy <= 16 each)
     } else {
         L.mid = take(sizeof(u32) * (n + 1));
@@ -132,6 +132,8 @@ ktri::Options resolve(const ktri_opts* o) {
     if (o->binary_intersection_cutoff) r.binary_cutoff = o->binary_intersection_cutoff;
     if (o->hybrid_cutoff_scale > 0) r.hybrid_scale = o->hybrid_cutoff_scale;
     r.force_wide = o->force_wide_offsets != 0;
+    if (o->medium_outdegree) r.medium_outdegree = o->medium_outdegree;
+    if (o->segment) r.segment = o->segment;
     return r;
 }
 
@@ -195,9 +197,9 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
     auto* mtiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
-    auto* ltiles = autom ? mtiles + ktri::large_tile_capacity(n, nnz, ktri::SMALL_D) : nullptr;
-    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? (u32)ktri::SMALL_D : 0xFFFFFFFFu,
-                            (u32)ktri::MEDIUM_D, ktri::LARGE_SEG, ctl, sms, st);
+    auto* ltiles = autom ? mtiles + ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment) : nullptr;
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
+                            opt.medium_outdegree, opt.segment, ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -209,9 +211,9 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, cnt,
-                                                   partials, ctl, sms, st, events ? ctx->ev[4] : nullptr,
-                                                   events ? ctx->ev[5] : nullptr));
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles,
+                                                   opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
+                                                   events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
         ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
     } else {
         const int grid = ktri::count_grid_edges(sms);
@@ -254,8 +256,12 @@ int check_common(ktri_ctx* ctx, const void* fo, const void* head, u64 n, u64 nnz
     if (n == 0 && nnz != 0) return set_error(ctx, KTRI_ERR_INVALID_CSR, "nnz > 0 with n == 0");
     if (opt.method < KTRI_METHOD_AUTO || opt.method > KTRI_METHOD_HYBRID)
         return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "unknown intersection method");
-    if (opt.method == KTRI_METHOD_AUTO && opt.small_outdegree != (u32)ktri::SMALL_D)
-        return set_error(ctx, KTRI_ERR_UNSUPPORTED, "small_outdegree other than 32 is not built in");
+    if (opt.small_outdegree < 1 || opt.small_outdegree > (u32)ktri::SMALL_D)
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "small_outdegree must be in 1..32");
+    if (opt.medium_outdegree < opt.small_outdegree || opt.medium_outdegree > (u32)ktri::MEDIUM_D)
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "medium_outdegree must be in small_outdegree..256");
+    if (opt.segment < ktri::MIN_SEG || opt.segment > ktri::LARGE_SEG || (opt.segment & (opt.segment - 1)))
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "segment must be a power of two in 64..1024");
     return KTRI_OK;
 }
 
@@ -345,7 +351,7 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
     auto* partials = reinterpret_cast<u64*>(base + L.partials);
     auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
     auto* mtiles = reinterpret_cast<uint2*>(base + L.ltiles);
-    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, ktri::SMALL_D);
+    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, (u32)ktri::SMALL_D, ktri::LARGE_SEG);
     // the control block (counters, error word) must start at zero; k_prep zeroes the
     // out-degrees and per-vertex counts; every other region is fully written before it is read
     if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return KTRI_ERR_CUDA;
@@ -353,8 +359,8 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, (u32)ktri::SMALL_D, (u32)ktri::MEDIUM_D,
                             ktri::LARGE_SEG, ctl, sms, st);
-    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, cnt, partials, ctl, sms,
-                                      st, nullptr, nullptr) != cudaSuccess)
+    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, (u32)ktri::SMALL_D,
+                                      ktri::LARGE_SEG, cnt, partials, ctl, sms, st, nullptr, nullptr) != cudaSuccess)
         return KTRI_ERR_CUDA;
     ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
@@ -365,6 +371,8 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
 }
 
 }  // namespace
+
+int ktri::ctx_device(const ktri_ctx* ctx) { return ctx->device; }
 
 extern "C" {
 
@@ -454,7 +462,8 @@ int ktri_count_csr_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint
         ctx->stats = ktri_run_stats{};
         return KTRI_OK;
     }
-    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, false, d_per_vertex == nullptr, opt.force_wide);
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, false, d_per_vertex == nullptr,
+                                 opt.force_wide, opt.small_outdegree, opt.segment);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex)
@@ -512,7 +521,8 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
     }
     if (first_out[0] != 0 || first_out[n] != nnz)
         return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
-    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide);
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true,
+                                 opt.force_wide, opt.small_outdegree, opt.segment);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->ws);
@@ -551,6 +561,98 @@ int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, 
         }
     }
     return ktri_count_csr_ctx(ctx, first_out, head, n, nnz, total_out, per_vertex_out, opts);
+}
+
+// ---- oriented lists (the katric local phase) ---------------------------------------------
+
+int ktri_count_dag_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t m,
+                          uint64_t* d_total, uint64_t* d_per_vertex, const ktri_opts* opts, void* stream) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_common(ctx, d_first_out, d_head, n, m, d_total, opt);
+    if (rc) return rc;
+    if (m > (1ull << 62)) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "too many edges");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        KTRI_CK(ctx, cudaMemsetAsync(d_total, 0, sizeof(u64), st));
+        ctx->pending = false;
+        ctx->stats = ktri_run_stats{};
+        return KTRI_OK;
+    }
+    const u64 nnz = 2 * m;
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, d_per_vertex == nullptr, opt.force_wide,
+                                 opt.small_outdegree, opt.segment);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* fs = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* hs = reinterpret_cast<u32*>(base + L.in_head);
+    // the out-list and descriptor regions are free until orientation starts: in-list cursors
+    // and scan sums live there meanwhile
+    auto* cursor = reinterpret_cast<u32*>(base + L.deg);
+    auto* sums = reinterpret_cast<u64*>(base + L.headp);
+    ktri::launch_dag_symmetrize(reinterpret_cast<const u64*>(d_first_out), d_head, n, fs, hs, cursor, sums,
+                                ctx->num_sms, st);
+    KTRI_CK(ctx, cudaGetLastError());
+    u64* cnt = d_per_vertex ? reinterpret_cast<u64*>(d_per_vertex) : reinterpret_cast<u64*>(base + L.cnt);
+    auto* tot = reinterpret_cast<u64*>(d_total);
+    return L.wide ? run_pipeline<u64>(ctx, L, fs, hs, n, nnz, tot, cnt, opt, st, false)
+                  : run_pipeline<u32>(ctx, L, fs, hs, n, nnz, tot, cnt, opt, st, false);
+}
+
+int ktri_count_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t m,
+                       uint64_t* total_out, uint64_t* per_vertex_out, const ktri_opts* opts) {
+    const ktri::Options opt = resolve(opts);
+    int rc = check_common(ctx, first_out, head, n, m, total_out, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    if (n == 0) {
+        *total_out = 0;
+        return KTRI_OK;
+    }
+    if (first_out[0] != 0 || first_out[n] != m)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal m");
+    for (u64 v = 0; v < n; ++v)
+        if (first_out[v + 1] < first_out[v])
+            return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out is not monotone");
+    if (m > (1ull << 62)) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "too many edges");
+    const u64 nnz = 2 * m;
+    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide, opt.small_outdegree,
+                                 opt.segment);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    // the caller's lists, the in-list cursors and the scan sums sit in the out-list region
+    // (at least 4 (2m + 3n + 8) bytes) until orientation overwrites it
+    char* scratch = base + L.headp;
+    auto* dfo = reinterpret_cast<u64*>(scratch);
+    const size_t off_head = align_up(sizeof(u64) * (n + 1));
+    auto* dhead = reinterpret_cast<u32*>(scratch + off_head);
+    auto* sums = reinterpret_cast<u64*>(scratch + align_up(off_head + sizeof(u32) * m));
+    if (align_up(off_head + sizeof(u32) * m) + sizeof(u64) * (ktri::dag_scan_chunks(n) + 1) >
+        sizeof(u32) * ktri::oriented_capacity(n, nnz))
+        return set_error(ctx, KTRI_ERR_UNSUPPORTED, "workspace layout too small for the oriented lists");
+    auto* fs = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* hs = reinterpret_cast<u32*>(base + L.in_head);
+    auto* cursor = reinterpret_cast<u32*>(base + L.deg);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemcpyAsync(dfo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (m) KTRI_CK(ctx, cudaMemcpyAsync(dhead, head, sizeof(u32) * m, cudaMemcpyHostToDevice, st));
+    ktri::launch_dag_symmetrize(dfo, dhead, n, fs, hs, cursor, sums, ctx->num_sms, st);
+    KTRI_CK(ctx, cudaGetLastError());
+    rc = L.wide ? run_pipeline<u64>(ctx, L, fs, hs, n, nnz, d_total, d_cnt, opt, st, false)
+                : run_pipeline<u32>(ctx, L, fs, hs, n, nnz, d_total, d_cnt, opt, st, false);
+    if (rc) return rc;
+    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
+    if (per_vertex_out)
+        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
+    return rc;
 }
 
 // ---- batches of graphs ----------------------------------------------------------------
@@ -613,7 +715,8 @@ int ktri_count_batch_device(ktri_ctx* ctx, const uint64_t* d_first_out, const ui
         ctx->pending = false;
         return KTRI_OK;
     }
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true, opt.force_wide);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true,
+                                 opt.force_wide, opt.small_outdegree, opt.segment);
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->ws);
@@ -649,7 +752,8 @@ int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_
     }
     if (first_out[0] != 0 || first_out[n_total] != nnz_total)
         return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, true, true, opt.force_wide);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, true, true,
+                                 opt.force_wide, opt.small_outdegree, opt.segment);
     const size_t off_gf = L.bytes, off_tot = align_up(off_gf + sizeof(u64) * (num_graphs + 1));
     const size_t total_bytes = align_up(off_tot + sizeof(u64) * (num_graphs + 1));
     rc = ensure_ws(ctx, total_bytes);
@@ -703,7 +807,8 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
     if (n_total == 0) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "a plan needs at least one vertex");
     DeviceGuard g(ctx->device);
     if (ctx->pending) device_status(ctx);
-    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true, opt.force_wide);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, true,
+                                 opt.force_wide, opt.small_outdegree, opt.segment);
     if (ctx->budget && L.bytes > ctx->budget)
         return set_error(ctx, KTRI_ERR_OUT_OF_MEMORY, "plan workspace exceeds the memory budget");
     ktri_plan* p = new (std::nothrow) ktri_plan();

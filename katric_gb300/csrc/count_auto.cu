@@ -12,16 +12,21 @@
 // owner's table: its hits accumulate in a shared-memory counter next to the key and are
 // flushed once per table.  y gets one atomic per edge, x one per tile.
 //
-// Two kernels split the owners by out-degree:
-//   k_count_small: owners with out-degree <= SMALL_D.  Merge-path tiles over the adjacency
-//     (as in orientation) give every block the same number of slots; the tables of all
-//     owners in a tile live side by side in shared memory.  Selected edges are queued,
+// Three kernels split the owners by out-degree (the bounds are runtime options, at most
+// SMALL_D and MEDIUM_D):
+//   k_count_small: owners with out-degree <= small_outdegree.  Merge-path tiles over the
+//     adjacency (as in orientation) give every block the same number of slots; the tables of
+//     all owners in a tile live side by side in shared memory.  Selected edges are queued,
 //     counting-sorted by streamed-list length so that the lanes of a warp carry equal work,
 //     then streamed one list per thread with uint4 loads.
-//   k_count_large: owners above SMALL_D, one (owner, segment of LARGE_SEG slots) tile per
-//     block iteration.  Short streamed lists are handled one per thread while the segment is
-//     scanned; longer ones are queued and taken one at a time by whole warps (one entry per
-//     lane, eight loads in flight), so no block-wide barrier separates the lists.
+//   k_count_medium: owners up to medium_outdegree, one warp per (owner, segment) tile with
+//     the warp's own table, filter and survivor buffer, so tiles need no block barrier.
+//   k_count_large: larger owners, one (owner, segment) tile per block iteration.  Short
+//     streamed lists are handled one per thread while the segment is scanned; longer ones are
+//     queued and taken one at a time by whole warps (one entry per lane, eight loads in
+//     flight), so no block-wide barrier separates the lists.
+// The medium and large kernels test every streamed entry against a one-hash filter of the
+// owner's keys first and look up only the survivors, packed 32 at a time.
 #include "ktri_device.cuh"
 #include "ktri_kernels.h"
 
@@ -52,8 +57,9 @@ template <int BLOCK, int IPT, int SD, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
                                                        const u32* __restrict__ headp,
-                                                       const u32* __restrict__ tile_i0, u64* __restrict__ cnt,
-                                                       u64* __restrict__ partials, Control* ctl) {
+                                                       const u32* __restrict__ tile_i0, u32 sd,
+                                                       u64* __restrict__ cnt, u64* __restrict__ partials,
+                                                       Control* ctl) {
     using L = SmallLayout<BLOCK, IPT, SD, OffT>;
     static_assert(L::TILE == TILE_BASE, "one counting tile = one base tile");
     constexpr int TILE = L::TILE;
@@ -127,7 +133,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             packed[r] = 0;
             if (k < nw) {
                 const u32 d = s_desc[k].d;
-                if (s_fo[k] < s_fo[k + 1] && d > 0 && d <= (u32)SD) {
+                if (s_fo[k] < s_fo[k + 1] && d > 0 && d <= sd) {
                     u32 lg = ceil_log2(2 * d);
                     if (lg < 2) lg = 2;
                     packed[r] = ((1u << lg) << 16) | d;
@@ -197,7 +203,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
                     if (i < n && j < s_fo[i + 1 - i0]) {
                         const u32 o = (u32)(i - i0);
                         const u32 d = s_desc[o].d;
-                        if (d > 0 && d <= (u32)SD) {
+                        if (d > 0 && d <= sd) {
                             own[k] = o;
                             yv[k] = __ldg(head + j0 + j);
                         }
@@ -434,8 +440,9 @@ template <int BLOCK, int CAP, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, const Desc<OffT>* __restrict__ vdesc,
                                                        const u32* __restrict__ headp,
-                                                       const uint2* __restrict__ ltiles, u64* __restrict__ cnt,
-                                                       u64* __restrict__ partials, Control* ctl) {
+                                                       const uint2* __restrict__ ltiles, u32 seg,
+                                                       u64* __restrict__ cnt, u64* __restrict__ partials,
+                                                       Control* ctl) {
     using L = LargeLayout<BLOCK, CAP, OffT>;
     constexpr int NW = BLOCK / 32;
     constexpr int U = 8;  // loads in flight per lane and list
@@ -468,8 +475,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         const Desc<OffT> dxd = load_desc(vdesc + x);
         const u32 dx = dxd.d;
         const u64 fx1 = fo[x + 1];
-        const u64 a = fo[x] + (u64)tl.y * LARGE_SEG;
-        const u64 b = a + LARGE_SEG < fx1 ? a + LARGE_SEG : fx1;
+        const u64 a = fo[x] + (u64)tl.y * seg;
+        const u64 b = a + seg < fx1 ? a + seg : fx1;
         u64 T = 0;
         for (u32 c0 = 0; c0 < dx; c0 += CAP) {
             const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
@@ -579,8 +586,8 @@ template <int BLOCK, typename OffT>
 __global__ void __launch_bounds__(BLOCK)
     k_count_medium(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
                    const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp,
-                   const uint2* __restrict__ mtiles, u64* __restrict__ cnt, u64* __restrict__ partials,
-                   Control* ctl) {
+                   const uint2* __restrict__ mtiles, u32 seg, u64* __restrict__ cnt,
+                   u64* __restrict__ partials, Control* ctl) {
     using L = MediumLayout<BLOCK>;
     constexpr int U = 8;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -606,8 +613,8 @@ __global__ void __launch_bounds__(BLOCK)
         const Desc<OffT> dxd = load_desc(vdesc + x);
         const u32 dx = dxd.d;
         const u64 fx1 = fo[x + 1];
-        const u64 a = fo[x] + (u64)tl.y * LARGE_SEG;
-        const u64 b = a + LARGE_SEG < fx1 ? a + LARGE_SEG : fx1;
+        const u64 a = fo[x] + (u64)tl.y * seg;
+        const u64 b = a + seg < fx1 ? a + seg : fx1;
         u32 lg, fl;
         chunk_sizes(dx, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FW * 32)), &lg, &fl);
         const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
@@ -814,20 +821,22 @@ int count_grid_auto(int num_sms) {
 
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u64* cnt, u64* partials,
-                              Control* ctl, int num_sms, cudaStream_t st, cudaEvent_t after_small,
-                              cudaEvent_t after_large) {
+                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
+                              u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
+                              cudaEvent_t after_small, cudaEvent_t after_large) {
     const int gs = count_grid_small<OffT>(num_sms);
     const int gm = count_grid_medium<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
     k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
-        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, cnt, partials, ctl);
+        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials,
+                                                       ctl);
     if (after_small) cudaEventRecord(after_small, st);
     k_count_medium<MEDIUM_BLOCK, OffT>
-        <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, cnt, partials + gs, ctl);
+        <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, seg, cnt, partials + gs, ctl);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
-        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, cnt, partials + gs + gm, ctl);
+        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, seg, cnt, partials + gs + gm,
+                                                       ctl);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
 }
@@ -860,10 +869,10 @@ template int count_grid_medium<u64>(int);
 template int count_grid_auto<u32>(int);
 template int count_grid_auto<u64>(int);
 template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const uint2*,
+                                            const uint2*, const uint2*, u32, u32,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const uint2*,
+                                            const uint2*, const uint2*, u32, u32,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
 template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
 template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);

@@ -18,12 +18,17 @@ namespace ktri {
 // Resolved options (defaults filled in).
 struct Options {
     int32_t method = KTRI_METHOD_AUTO;
-    uint32_t small_outdegree = 32;
+    uint32_t small_outdegree = 32;   // owner bins and tile segment of the AUTO kernels
+    uint32_t medium_outdegree = 256;
+    uint32_t segment = 1024;
     bool collect_stats = false;
     uint64_t binary_cutoff = 1000;
     double hybrid_scale = 1.0;
     bool force_wide = false;
 };
+
+// The device a context was created on.
+int ctx_device(const ktri_ctx* ctx);
 
 // Device-side error bits written by the kernels (one u32 word in the control block).
 enum : uint32_t {

@@ -21,20 +21,24 @@ constexpr int MEDIUM_D = 256;        // out-degree bound of the warp-per-tile ke
 constexpr int MEDIUM_BLOCK = 256;
 constexpr int LARGE_BLOCK = 256;
 constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of the vertex kernel
-constexpr u32 LARGE_SEG = 1024;      // adjacency slots per (owner, segment) tile
+constexpr u32 LARGE_SEG = 1024;      // most adjacency slots per (owner, segment) tile
+constexpr u32 MIN_SEG = 64;          // fewest adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
 // Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
 // the vertex where diagonal k * TILE_BASE crosses the path.  The counting tiles are one base
-// tile, the orientation tiles two.
-constexpr u64 TILE_BASE = 768;
-static_assert(ORIENT_BLOCK * ORIENT_IPT == 2 * TILE_BASE, "orientation tile = 2 base tiles");
+// tile, the orientation tiles ORIENT_PER_BASE of them.
+constexpr u64 TILE_BASE = (u64)SMALL_BLOCK * SMALL_IPT;
+constexpr u64 ORIENT_PER_BASE = (u64)ORIENT_BLOCK * ORIENT_IPT / TILE_BASE;
+static_assert(ORIENT_PER_BASE * TILE_BASE == (u64)ORIENT_BLOCK * ORIENT_IPT, "orientation tile = whole base tiles");
 inline u64 base_tiles(u64 n, u64 nnz) { return (n + nnz + TILE_BASE - 1) / TILE_BASE; }
-inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d) {
+// Owners above small_d hold more than small_d adjacency entries each; every owner has at most
+// deg / seg + 1 tiles.
+inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d, u32 seg) {
     u64 owners = nnz / ((u64)small_d + 1) + 1;
     if (owners > n) owners = n;
-    return owners + nnz / LARGE_SEG + 1;
+    return owners + nnz / seg + 1;
 }
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
@@ -58,10 +62,16 @@ template <typename OffT>
 int count_grid_auto(int num_sms);  // small + medium + large
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u64* cnt, u64* partials,
-                              Control* ctl, int num_sms,
-                              cudaStream_t st, cudaEvent_t after_small, cudaEvent_t after_large);
+                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
+                              u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
+                              cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
+
+// Oriented out-lists -> undirected CSR of their edges (fs: n + 1 offsets, hs: 2m ids).  cursor
+// needs n u32 and sums dag_scan_chunks(n) u64 of scratch.
+u64 dag_scan_chunks(u64 n);
+void launch_dag_symmetrize(const u64* fo, const u32* head, u64 n, u64* fs, u32* hs, u32* cursor, u64* sums,
+                           int num_sms, cudaStream_t st);
 void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs, u64 n, u64* totals, Control* ctl,
                          int num_sms, cudaStream_t st);
 

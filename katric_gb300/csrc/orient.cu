@@ -66,8 +66,8 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     const u64 d1 = d0 + TILE < total ? d0 + TILE : total;
     if (threadIdx.x == 0) {
         const u64 nt = (total + TILE_BASE - 1) / TILE_BASE;
-        const u64 k1 = 2 * (u64)blockIdx.x + 2;
-        s_b[0] = tile_i0[2 * (u64)blockIdx.x];
+        const u64 k1 = ORIENT_PER_BASE * ((u64)blockIdx.x + 1);
+        s_b[0] = tile_i0[ORIENT_PER_BASE * (u64)blockIdx.x];
         s_b[1] = tile_i0[k1 < nt ? k1 : nt];
     }
     __syncthreads();

@@ -8,7 +8,8 @@
 // the requests that arrived meanwhile and launched on a free slot, so the work of batches
 // overlaps on the GPU.  Graphs stay resident (CSR and counts on the device, keyed by the
 // caller's graph key) until the memory budget needs their room; a repeated request for a
-// resident graph is answered from the resident counts without counting again.
+// resident graph is answered from the resident counts without counting again, and one for a
+// graph that is still queued or counting waits for that count instead of starting another.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,6 +44,15 @@ __global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64
     }
 }
 
+// The caller's own CSR of one graph of a rebased union (the inverse of k_rebase for it).
+__global__ void k_unbase(u64* __restrict__ dfo, u32* __restrict__ dhead, const u64* __restrict__ sfo,
+                         const u32* __restrict__ shead, u64 n, u64 nnz, u64 vb, u64 eb) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    const u64 i0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (u64 i = i0; i <= n; i += stride) dfo[i] = sfo[vb + i] - eb;
+    for (u64 i = i0; i < nnz; i += stride) dhead[i] = shead[eb + i] - (u32)vb;
+}
+
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -60,6 +70,8 @@ struct Request {
     int status = KTRI_OK;
     uint64_t total = 0;
     std::vector<uint64_t> pv;
+    std::vector<Request*> followers;  // later requests for the same key, answered with this one
+    bool follower_pv = false;         // a follower wants the per-vertex counts
 };
 
 struct Resident {  // a graph kept on the device with its counts
@@ -105,6 +117,7 @@ struct ktri_server {
     cudaStream_t aux = nullptr;  // cache copies
     // resident graphs
     std::unordered_map<uint64_t, Resident> resident;
+    std::unordered_map<uint64_t, Request*> leaders;  // key -> the queued or counting request for it
     std::list<uint64_t> lru;  // front = most recent
     size_t resident_bytes = 0;
     ktri_server_stats st{};
@@ -142,6 +155,19 @@ void finish(ktri_server* s, Request* r, int status) {
     r->t_done = now_s();
     r->done = true;
     s->st.completed++;
+    if (r->key) {
+        auto it = s->leaders.find(r->key);
+        if (it != s->leaders.end() && it->second == r) s->leaders.erase(it);
+    }
+    for (Request* f : r->followers) {
+        f->total = r->total;
+        if (f->want_pv && status == KTRI_OK) f->pv = r->pv;
+        f->status = status;
+        f->t_done = r->t_done;
+        f->done = true;
+        s->st.completed++;
+    }
+    r->followers.clear();
 }
 
 // Answer a request for a resident graph from its resident counts.
@@ -160,7 +186,9 @@ void serve_resident(ktri_server* s, Request* r, Resident& res) {
     s->st.cache_hits++;
 }
 
-// Keep a counted graph resident (CSR + counts on the device), room permitting.
+// Keep a counted graph resident (CSR + counts on the device), room permitting.  The copy is
+// taken on the device from the slot's union, on the auxiliary stream, which the slot's next
+// batch waits for (cache_done) before it overwrites the union.
 void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 ebase, size_t inflight) {
     if (!r->key || s->resident.count(r->key)) return;
     const size_t bytes = al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)) + al(8 * (r->n + 1));
@@ -174,11 +202,14 @@ void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 eb
     char* b = static_cast<char*>(mem);
     const char* d = static_cast<const char*>(sl.dev);
     // the slot's union holds rebased ids; the resident copy keeps the caller's own CSR
-    cudaMemcpyAsync(b, r->bfo, 8 * (r->n + 1), cudaMemcpyHostToDevice, s->aux);
-    if (r->nnz) cudaMemcpyAsync(b + al(8 * (r->n + 1)), r->bhead, 4 * r->nnz, cudaMemcpyHostToDevice, s->aux);
-    cudaMemcpyAsync(b + al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)), d + sl.off_pv + 8 * vbase, 8 * r->n,
-                    cudaMemcpyDeviceToDevice, s->aux);
-    (void)ebase;
+    const u64 items = std::max<u64>(r->n + 1, r->nnz);
+    const unsigned blocks = (unsigned)std::min<u64>((items + 255) / 256, 2048);
+    k_unbase<<<blocks, 256, 0, s->aux>>>(reinterpret_cast<u64*>(b), reinterpret_cast<u32*>(b + al(8 * (r->n + 1))),
+                                         reinterpret_cast<const u64*>(d + sl.off_fo),
+                                         reinterpret_cast<const u32*>(d + sl.off_head), r->n, r->nnz, vbase, ebase);
+    if (r->n)
+        cudaMemcpyAsync(b + al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)), d + sl.off_pv + 8 * vbase, 8 * r->n,
+                        cudaMemcpyDeviceToDevice, s->aux);
     Resident res;
     res.key = r->key;
     res.n = r->n;
@@ -311,7 +342,7 @@ void harvest(ktri_server* s, Slot& sl) {
         Request* r = sl.reqs[i];
         if (rc == KTRI_OK) {
             r->total = tot[i];
-            if (r->want_pv) r->pv.assign(pv + vb, pv + vb + r->n);
+            if (r->want_pv || r->follower_pv) r->pv.assign(pv + vb, pv + vb + r->n);
             keep_resident(s, r, sl, vb, eb, inflight);
         }
         vb += r->n;
@@ -493,7 +524,28 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     }
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stop) return KTRI_ERR_INVALID_ARGUMENT;
-    if (!first_out && !s->resident.count(graph_key)) return KTRI_ERR_INVALID_ARGUMENT;
+    const bool resident = graph_key && s->resident.count(graph_key);
+    auto lead = graph_key && !resident ? s->leaders.find(graph_key) : s->leaders.end();
+    // a request for a key that is queued or counting joins that count (same graph size only)
+    if (lead != s->leaders.end() && (!first_out || (lead->second->n == n && lead->second->nnz == nnz))) {
+        Request* l = lead->second;
+        r->n = l->n;
+        r->nnz = l->nnz;
+        r->fo.clear();
+        r->head.clear();
+        r->bfo = nullptr;
+        r->bhead = nullptr;
+        r->id = s->next_id++;
+        r->t_submit = now_s();
+        *request_id = r->id;
+        l->follower_pv |= r->want_pv;
+        l->followers.push_back(r.get());
+        s->requests.emplace(r->id, std::move(r));
+        s->st.submitted++;
+        s->st.coalesced++;
+        return KTRI_OK;
+    }
+    if (!first_out && !resident) return KTRI_ERR_INVALID_ARGUMENT;
     if (!first_out) {
         const Resident& res = s->resident.at(graph_key);
         r->n = res.n;
@@ -502,6 +554,7 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     r->id = s->next_id++;
     r->t_submit = now_s();
     *request_id = r->id;
+    if (graph_key && !resident && lead == s->leaders.end()) s->leaders[graph_key] = r.get();
     s->pending.push_back(r.get());
     s->requests.emplace(r->id, std::move(r));
     s->st.submitted++;

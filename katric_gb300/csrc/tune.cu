@@ -1,0 +1,291 @@
+// Autotuner of the counting configuration: intersection strategy, owner-bin thresholds and
+// the owner tile segment.  It times candidate configurations of one count (a single graph or
+// a packed batch) on the caller's device buffers, keeps the fastest, and persists the choice
+// per shape class in a JSON-lines cache file, so later runs on inputs of the same class read
+// it back without timing.
+//
+// Search: the library default (KTRI_METHOD_AUTO with bins 32 / 256, segment 1024) is timed
+// first; then the reference's strategies (hybrid first; merge, binary search and binary only
+// when hybrid comes within 1.5x of the best); then, if an AUTO configuration is best, one pass
+// of coordinate descent over small_outdegree, medium_outdegree and segment.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "ktri.h"
+#include "ktri_internal.h"
+
+namespace {
+
+using u64 = unsigned long long;
+
+__global__ void k_max_degree(const u64* __restrict__ fo, u64 n, u64* __restrict__ out) {
+    u64 m = 0;
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 v = (u64)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        const u64 d = fo[v + 1] - fo[v];
+        m = d > m ? d : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const u64 y = __shfl_xor_sync(0xFFFFFFFFu, m, o);
+        m = y > m ? y : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+int floor_log2(u64 x) {
+    int r = 0;
+    while (x >>= 1) ++r;
+    return r;
+}
+
+struct Cand {
+    int32_t method = KTRI_METHOD_AUTO;
+    uint32_t small = 32, medium = 256, seg = 1024;
+    bool operator==(const Cand& o) const {
+        return method == o.method && small == o.small && medium == o.medium && seg == o.seg;
+    }
+};
+
+// Reads the last line of the cache whose signature matches.
+bool read_cache(const char* path, const std::string& sig, Cand* c, double* ms) {
+    std::ifstream f(path);
+    if (!f) return false;
+    const std::string key = "\"signature\": \"" + sig + "\"";
+    std::string line;
+    bool found = false;
+    auto field = [](const std::string& l, const char* name, double* v) {
+        const std::string k = std::string("\"") + name + "\": ";
+        const size_t p = l.find(k);
+        if (p == std::string::npos) return false;
+        *v = std::strtod(l.c_str() + p + k.size(), nullptr);
+        return true;
+    };
+    while (std::getline(f, line)) {
+        if (line.find(key) == std::string::npos) continue;
+        double m, s, md, sg, t;
+        if (!field(line, "method", &m) || !field(line, "small_outdegree", &s) ||
+            !field(line, "medium_outdegree", &md) || !field(line, "segment", &sg) || !field(line, "ms", &t))
+            continue;
+        c->method = (int32_t)m;
+        c->small = (uint32_t)s;
+        c->medium = (uint32_t)md;
+        c->seg = (uint32_t)sg;
+        *ms = t;
+        found = true;
+    }
+    return found;
+}
+
+bool append_cache(const char* path, const std::string& sig, const Cand& c, double ms, double default_ms,
+                  uint32_t candidates) {
+    FILE* f = std::fopen(path, "a");
+    if (!f) return false;
+    std::fprintf(f,
+                 "{\"signature\": \"%s\", \"method\": %d, \"small_outdegree\": %u, \"medium_outdegree\": %u, "
+                 "\"segment\": %u, \"ms\": %.6f, \"default_ms\": %.6f, \"candidates\": %u, \"version\": \"%s\"}\n",
+                 sig.c_str(), c.method, c.small, c.medium, c.seg, ms, default_ms, candidates, ktri_version());
+    return std::fclose(f) == 0;
+}
+
+}  // namespace
+
+extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n,
+                             uint64_t nnz, const uint64_t* d_graph_first, uint64_t num_graphs, const char* cache_path,
+                             ktri_opts* opts, ktri_tuning* out, void* stream) {
+    if (!ctx || !opts || !out || (n && !d_first_out) || (nnz && !d_head) || (d_graph_first && !num_graphs))
+        return KTRI_ERR_INVALID_ARGUMENT;
+    if (n == 0) return KTRI_ERR_INVALID_ARGUMENT;
+    const int device = ktri::ctx_device(ctx);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return KTRI_ERR_NO_DEVICE;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    ktri_opts base{};
+    base.struct_size = sizeof(ktri_opts);
+    if (opts->struct_size) std::memcpy(&base, opts, std::min<size_t>(sizeof(ktri_opts), opts->struct_size));
+    base.struct_size = sizeof(ktri_opts);
+    base.collect_stats = 0;
+
+    int rc = KTRI_OK;
+    u64* d_tmp = nullptr;  // [0] max degree, then per-graph totals
+    const u64 k = d_graph_first ? num_graphs : 1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ktri_tuning res{};
+    res.struct_size = sizeof(ktri_tuning);
+    do {
+        if (cudaMalloc(&d_tmp, sizeof(u64) * (k + 1)) != cudaSuccess) {
+            cudaGetLastError();
+            rc = KTRI_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        cudaMemsetAsync(d_tmp, 0, sizeof(u64), st);
+        const unsigned blocks = (unsigned)std::min<u64>((n + 255) / 256, 4096);
+        k_max_degree<<<blocks, 256, 0, st>>>(reinterpret_cast<const u64*>(d_first_out), n, d_tmp);
+        u64 maxdeg = 0;
+        if (cudaMemcpyAsync(&maxdeg, d_tmp, sizeof(u64), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            cudaGetLastError();
+            rc = KTRI_ERR_CUDA;
+            break;
+        }
+        int sms = 0, ccmaj = 0, ccmin = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        cudaDeviceGetAttribute(&ccmaj, cudaDevAttrComputeCapabilityMajor, device);
+        cudaDeviceGetAttribute(&ccmin, cudaDevAttrComputeCapabilityMinor, device);
+        char sig[96];
+        std::snprintf(sig, sizeof(sig), "cc%d%d-sm%d-g%d-n%d-e%d-d%d", ccmaj, ccmin, sms, floor_log2(k),
+                      floor_log2(n), floor_log2(nnz ? nnz : 1), floor_log2(maxdeg ? maxdeg : 1));
+        std::snprintf(res.signature, sizeof(res.signature), "%s", sig);
+
+        Cand best;
+        double best_ms = 0;
+        if (cache_path && read_cache(cache_path, sig, &best, &best_ms)) {
+            res.from_cache = 1;
+            res.ms = best_ms;
+        } else {
+            if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+                cudaGetLastError();
+                rc = KTRI_ERR_CUDA;
+                break;
+            }
+            uint64_t* d_tot = reinterpret_cast<uint64_t*>(d_tmp + 1);
+            std::vector<std::pair<Cand, double>> seen;
+            // time one configuration: a warm-up call (it also sizes the workspace), then the
+            // fastest of up to three timed calls (one when a call takes over 50 ms)
+            auto timed = [&](const Cand& c, double* ms) -> int {
+                for (const auto& s : seen)
+                    if (s.first == c) {
+                        *ms = s.second;
+                        return KTRI_OK;
+                    }
+                ktri_opts o = base;
+                o.intersection_method = c.method;
+                o.small_outdegree = c.small;
+                o.medium_outdegree = c.medium;
+                o.segment = c.seg;
+                double bestt = 1e30;
+                for (int rep = 0; rep < 4; ++rep) {
+                    cudaEventRecord(e0, st);
+                    int r = d_graph_first
+                                ? ktri_count_batch_device(ctx, d_first_out, d_head, n, nnz, d_graph_first,
+                                                          num_graphs, d_tot, nullptr, &o, st)
+                                : ktri_count_csr_device(ctx, d_first_out, d_head, n, nnz, d_tot, nullptr, &o, st);
+                    if (r) return r;
+                    cudaEventRecord(e1, st);
+                    r = ktri_ctx_check(ctx);
+                    if (r) return r;
+                    float t = 0;
+                    cudaEventElapsedTime(&t, e0, e1);
+                    if (rep > 0) bestt = std::min(bestt, (double)t);
+                    if (rep >= 1 && t > 50.0f) break;
+                }
+                *ms = bestt;
+                seen.push_back({c, bestt});
+                res.candidates++;
+                return KTRI_OK;
+            };
+            Cand def;
+            double t = 0;
+            rc = timed(def, &best_ms);
+            if (rc) break;
+            res.default_ms = best_ms;
+            // the reference's strategies on id-sorted lists
+            Cand hy = def;
+            hy.method = KTRI_METHOD_HYBRID;
+            rc = timed(hy, &t);
+            if (rc) break;
+            if (t < best_ms) {
+                best = hy;
+                best_ms = t;
+            }
+            if (t < 1.5 * best_ms) {
+                for (int32_t m : {KTRI_METHOD_MERGE, KTRI_METHOD_BINARY_SEARCH, KTRI_METHOD_BINARY}) {
+                    Cand c = def;
+                    c.method = m;
+                    rc = timed(c, &t);
+                    if (rc) break;
+                    if (t < best_ms) {
+                        best = c;
+                        best_ms = t;
+                    }
+                }
+                if (rc) break;
+            }
+            if (best.method == KTRI_METHOD_AUTO) {
+                for (uint32_t s : {8u, 16u, 32u}) {
+                    Cand c = best;
+                    c.small = s;
+                    if (c.medium < s) c.medium = s;
+                    rc = timed(c, &t);
+                    if (rc) break;
+                    if (t < best_ms) {
+                        best = c;
+                        best_ms = t;
+                    }
+                }
+                if (rc) break;
+                for (uint32_t m : {64u, 128u, 256u}) {
+                    Cand c = best;
+                    c.medium = std::max(m, c.small);
+                    rc = timed(c, &t);
+                    if (rc) break;
+                    if (t < best_ms) {
+                        best = c;
+                        best_ms = t;
+                    }
+                }
+                if (rc) break;
+                for (uint32_t g : {256u, 512u, 1024u}) {
+                    Cand c = best;
+                    c.seg = g;
+                    rc = timed(c, &t);
+                    if (rc) break;
+                    if (t < best_ms) {
+                        best = c;
+                        best_ms = t;
+                    }
+                }
+                if (rc) break;
+            }
+            res.ms = best_ms;
+            if (cache_path && !append_cache(cache_path, sig, best, best_ms, res.default_ms, res.candidates)) {
+                rc = KTRI_ERR_IO;
+                break;
+            }
+        }
+        res.intersection_method = best.method;
+        res.small_outdegree = best.small;
+        res.medium_outdegree = best.medium;
+        res.segment = best.seg;
+    } while (false);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (d_tmp) {
+        cudaStreamSynchronize(st);
+        cudaFree(d_tmp);
+    }
+    cudaSetDevice(prev);
+    if (rc == KTRI_OK) {
+        const uint32_t keep = opts->struct_size ? opts->struct_size : (uint32_t)sizeof(ktri_opts);
+        ktri_opts o = base;
+        o.collect_stats = opts->struct_size ? opts->collect_stats : 0;
+        o.intersection_method = res.intersection_method;
+        o.small_outdegree = res.small_outdegree;
+        o.medium_outdegree = res.medium_outdegree;
+        o.segment = res.segment;
+        std::memcpy(opts, &o, std::min<size_t>(keep, sizeof(ktri_opts)));
+        opts->struct_size = keep;
+        *out = res;
+    }
+    return rc;
+}

@@ -101,3 +101,42 @@ def test_batch_device_entry_point(counter, oracle):
                                tot.data_ptr(), None)
     counter.check()
     assert np.array_equal(tot.cpu().numpy().view(np.uint64), et)
+
+
+def test_autotune_persists_and_plans_exactly(counter, oracle, tmp_path):
+    """The autotuner times strategies, bins and segments on the batch, persists the choice as a
+    JSON line, reads it back for an input of the same shape class, and the plan it configures
+    counts exactly."""
+    import json
+    torch = pytest.importorskip("torch")
+    b = Batch.generate(48, 6, 13, 4, 48, seed=17)
+    et, epv = oracle_batch(oracle, b)
+    fo, hd, gf = _dev(b.union.first_out, torch), _dev(b.union.head, torch), _dev(b.graph_first, torch)
+    cache = tmp_path / "tune.jsonl"
+    conf, info = counter.autotune(fo.data_ptr(), hd.data_ptr(), b.union.n, b.union.nnz, gf.data_ptr(),
+                                  b.num_graphs, cache_path=str(cache))
+    assert not info["from_cache"] and info["candidates"] >= 5 and info["ms"] <= info["default_ms"]
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    assert rec["signature"] == info["signature"] and rec["segment"] == conf.segment
+    assert rec["small_outdegree"] == conf.small_outdegree and rec["medium_outdegree"] == conf.medium_outdegree
+    conf2, info2 = counter.autotune(fo.data_ptr(), hd.data_ptr(), b.union.n, b.union.nnz, gf.data_ptr(),
+                                    b.num_graphs, cache_path=str(cache))
+    assert info2["from_cache"] and info2["candidates"] == 0 and conf2 == conf
+    tot = torch.zeros(b.num_graphs, dtype=torch.int64, device="cuda")
+    pv = torch.zeros(b.union.n, dtype=torch.int64, device="cuda")
+    plan = counter.plan_batch(fo.data_ptr(), hd.data_ptr(), b.union.n, b.union.nnz, gf.data_ptr(), b.num_graphs,
+                              tot.data_ptr(), pv.data_ptr(), conf)
+    plan.launch()
+    plan.check()
+    assert np.array_equal(tot.cpu().numpy().view(np.uint64), et)
+    assert np.array_equal(pv.cpu().numpy().view(np.uint64), epv)
+    plan.close()
+    # a single graph (no graph_first) tunes too
+    g = Graph.rmat(13, 16, seed=6)
+    gfo, ghd = _dev(g.first_out, torch), _dev(g.head, torch)
+    conf3, info3 = counter.autotune(gfo.data_ptr(), ghd.data_ptr(), g.n, g.nnz)
+    assert info3["candidates"] >= 5
+    t, p = counter.count(g.first_out, g.head, conf3)
+    assert t == oracle.count(g.first_out, g.head, num_threads=4)[0]

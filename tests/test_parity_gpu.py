@@ -138,6 +138,29 @@ def test_many_components_mixed(counter, oracle):
     check_parity(counter, oracle, np.array(fo, np.uint64), np.array(hd, np.uint32))
 
 
+@pytest.mark.parametrize("small,medium,segment", [(1, 1, 64), (8, 64, 128), (16, 256, 256), (32, 32, 512),
+                                                   (32, 128, 1024), (4, 200, 64)])
+def test_bin_thresholds_and_segments(counter, oracle, small, medium, segment):
+    """Every owner-bin split and tile segment gives the same counts (the autotuner's space)."""
+    graphs = [Graph.rmat(14, 16, seed=4), Graph.rgg2d(1 << 13, 24.0, seed=5)]
+    fo, hd = csr_from_edges(300, [(i, j) for i in range(300) for j in range(i + 1, 300)
+                                  if (i * 7 + j * 3) % 5 != 0])
+    for g_fo, g_hd in [(g.first_out, g.head) for g in graphs] + [(fo, hd)]:
+        total, pv, _ = oracle.count(g_fo, g_hd, method="merge", num_threads=8)
+        t, p = counter.count(g_fo, g_hd, Config(small_outdegree=small, medium_outdegree=medium, segment=segment))
+        assert t == total and np.array_equal(p, pv), (small, medium, segment)
+
+
+@pytest.mark.parametrize("bad", [dict(small_outdegree=33), dict(small_outdegree=16, medium_outdegree=8),
+                                 dict(medium_outdegree=257), dict(segment=100), dict(segment=32),
+                                 dict(segment=2048)])
+def test_bad_bin_options(counter, bad):
+    g = Graph.gnm(1 << 10, 1 << 13, seed=3)
+    with pytest.raises(KtriError) as e:
+        counter.count(g.first_out, g.head, Config(**bad))
+    assert e.value.code == _native.ERR_INVALID_ARGUMENT
+
+
 def test_invalid_csr(counter):
     fo = np.array([0, 2, 3, 4], dtype=np.uint64)
     with pytest.raises(KtriError) as e:  # self-loop 0-0

@@ -69,3 +69,34 @@ def test_memory_budget_evicts_and_refuses():
         rid = srv.submit(big, key=0)
         with TriangleCounter(0) as ctr:
             assert srv.wait(rid)[0] == ctr.count(big.first_out, big.head)[0]
+
+
+def test_repeats_while_queued_join_the_count():
+    """A request for a key that is still queued or counting is answered by that count; later
+    repeats are answered from the resident copy taken on the device from the batch union."""
+    big = Graph.rmat(17, 16, seed=9)
+    small = graph_mix(12, seed=77)
+    with TriangleCounter(0) as ctr:
+        want_big = ctr.count(big.first_out, big.head)
+        want_small = [ctr.count(g.first_out, g.head) for g in small]
+    with Server(slots=1) as srv:
+        first = srv.submit(big, key=5)
+        again = [srv.submit(big, key=5, borrow=True), srv.submit(None, key=5),
+                 srv.submit(big, key=5, per_vertex=False)]
+        mix = [srv.submit(g, key=100 + i) for i, g in enumerate(small)]
+        total, pv, _ = srv.wait(first)
+        assert total == want_big[0] and np.array_equal(pv, want_big[1])
+        for rid, wants_pv in zip(again, (True, True, False)):
+            total, pv, _ = srv.wait(rid)
+            assert total == want_big[0]
+            assert (pv is None) if not wants_pv else np.array_equal(pv, want_big[1])
+        for rid, w in zip(mix, want_small):
+            total, pv, _ = srv.wait(rid)
+            assert total == w[0] and np.array_equal(pv, w[1])
+        st = srv.stats()
+        assert st["coalesced"] + st["cache_hits"] == 3
+        assert st["batched_graphs"] == 1 + len(small)
+        later = [srv.submit(None, key=5)] + [srv.submit(None, key=100 + i) for i in range(len(small))]
+        for rid, w in zip(later, [want_big] + want_small):
+            total, pv, _ = srv.wait(rid)
+            assert total == w[0] and np.array_equal(pv, w[1])
