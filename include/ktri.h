@@ -171,6 +171,25 @@ int ktri_plan_launch(ktri_plan* plan, void* stream);
 int ktri_plan_check(ktri_plan* plan);
 int ktri_plan_destroy(ktri_plan* plan);
 
+/* ---- file ingest ---------------------------------------------------------------------------
+ * The reference's binary graph format (shmetric --input-format binary, read by graph-io:
+ * <stem>.first_out u64[n+1] and <stem>.head u64[nnz]) counted straight from the files: the
+ * files are read in chunks of chunk_bytes (0 = 64 MiB) into two pinned buffers while the other
+ * buffer's chunk is copied to the device, so the disk or page-cache read overlaps the transfer.
+ * ktri_binary_file_shape reports n and nnz from the file sizes (to size per_vertex_out). */
+int ktri_binary_file_shape(const char* stem, uint64_t* n_out, uint64_t* nnz_out);
+int ktri_count_binary_file(ktri_ctx* ctx, const char* stem, uint64_t* total_out, uint64_t* per_vertex_out,
+                           const ktri_opts* opts, uint64_t chunk_bytes);
+
+/* ---- triangle listing ----------------------------------------------------------------------
+ * The check run_shmem performs in debug builds (shared_memory_cetric.h:151-167: collect every
+ * emitted triangle, sort, look for duplicates) needs the triangles themselves.
+ * ktri_list_triangles writes up to `capacity` triangles as id triples (x < y < z, in no
+ * particular order) and the total count; with more triangles than capacity it fills the
+ * buffer, sets *count_out and returns KTRI_ERR_OUT_OF_MEMORY.  It runs the merge strategy. */
+int ktri_list_triangles(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                        uint32_t* triples_out, uint64_t capacity, uint64_t* count_out);
+
 /* ---- oriented lists: the katric local phase -----------------------------------------------
  * Replaces CetricEdgeIterator::run_local on one rank's graph (cetric_edge_iterator.h:173-227,
  * called from cetric.h:431,450 and :827,847), which walks lists the caller has already

@@ -130,6 +130,9 @@ SIGNATURES = {
     "ktri_plan_launch": (ctypes.c_int, [P, P]),
     "ktri_plan_check": (ctypes.c_int, [P]),
     "ktri_plan_destroy": (ctypes.c_int, [P]),
+    "ktri_binary_file_shape": (ctypes.c_int, [CP, ctypes.POINTER(U64), ctypes.POINTER(U64)]),
+    "ktri_count_binary_file": (ctypes.c_int, [P, CP, ctypes.POINTER(U64), P, ctypes.POINTER(Opts), U64]),
+    "ktri_list_triangles": (ctypes.c_int, [P, P, P, U64, U64, P, U64, ctypes.POINTER(U64)]),
     "ktri_count_dag_ctx": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts)]),
     "ktri_count_dag_device": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts), P]),
     "ktri_autotune": (ctypes.c_int, [P, P, P, U64, U64, P, U64, CP, ctypes.POINTER(Opts), ctypes.POINTER(Tuning), P]),

@@ -158,6 +158,37 @@ class TriangleCounter:
         self._check(self._L.ktri_count_csr_device(self._ctx, first_out_ptr, head_ptr, n, nnz, total_ptr,
                                                   per_vertex_ptr, ctypes.byref(opts), stream or None))
 
+    def count_binary_file(self, stem: str, conf: Config | None = None, per_vertex: bool = True,
+                          chunk_bytes: int = 0):
+        """Count <stem>.first_out / <stem>.head (the reference's binary format) straight from the
+        files; reads overlap the host-to-device copies.  Returns (total, per-vertex or None)."""
+        conf = conf or Config()
+        n, nnz = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        path = str(stem).encode()
+        _native.check(self._L.ktri_binary_file_shape(path, ctypes.byref(n), ctypes.byref(nnz)))
+        total = ctypes.c_uint64(0)
+        pv = np.zeros(max(1, n.value), dtype=np.uint64) if per_vertex else None
+        opts = conf.opts()
+        self._check(self._L.ktri_count_binary_file(self._ctx, path, ctypes.byref(total),
+                                                   pv.ctypes.data if pv is not None else None, ctypes.byref(opts),
+                                                   chunk_bytes))
+        return int(total.value), (pv[: n.value] if pv is not None else None)
+
+    def list_triangles(self, first_out, head, capacity: int | None = None) -> np.ndarray:
+        """All triangles as a (count, 3) u32 array of ids x < y < z (unordered rows): the
+        debug check of run_shmem (shared_memory_cetric.h:151-167).  With capacity=None the
+        count is taken first."""
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, nnz = len(fo) - 1, len(hd)
+        if capacity is None:
+            capacity = self.count(fo, hd, Config(intersection_method="merge"), per_vertex=False)[0]
+        out = np.zeros((max(1, capacity), 3), dtype=np.uint32)
+        count = ctypes.c_uint64(0)
+        self._check(self._L.ktri_list_triangles(self._ctx, fo.ctypes.data, hd.ctypes.data if nnz else None, n, nnz,
+                                                out.ctypes.data, capacity, ctypes.byref(count)))
+        return out[: int(count.value)]
+
     def count_dag(self, first_out, head, conf: Config | None = None, per_vertex: bool = True):
         """CetricEdgeIterator::run_local on lists the caller oriented (out_adj of local vertices,
         ghost_adj of ghosts): the triangles whose three edges appear in the lists.

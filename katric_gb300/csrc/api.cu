@@ -1,5 +1,8 @@
 // C ABI: contexts, workspace management and the counting entry points.
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -180,7 +183,8 @@ struct DeviceGuard {
 
 template <typename OffT>
 int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz,
-                     u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all, bool events) {
+                     u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all, bool events,
+                     ktri::TriangleSink sink = ktri::TriangleSink{}) {
     auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
     auto* deg = reinterpret_cast<u32*>(base + L.deg);
     auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
@@ -218,7 +222,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     } else {
         const int grid = ktri::count_grid_edges(sms);
         ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
-                                       grid, ctl, st);
+                                       grid, ctl, sink, st);
         ktri::launch_final(partials, (u32)grid, d_total, ctl, st);
     }
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[3], st));
@@ -229,9 +233,10 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
 // Enqueue a count on the context's workspace and remember it for ktri_ctx_check / stats.
 template <typename OffT>
 int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total,
-                 u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all) {
+                 u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all,
+                 ktri::TriangleSink sink = ktri::TriangleSink{}) {
     char* base = static_cast<char*>(ctx->ws);
-    const int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, sort_all, true);
+    const int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, sort_all, true, sink);
     if (rc) return rc;
     ctx->ctl = reinterpret_cast<Control*>(base + L.ctl);
     ctx->last_stream = st;
@@ -563,6 +568,174 @@ int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, 
     return ktri_count_csr_ctx(ctx, first_out, head, n, nnz, total_out, per_vertex_out, opts);
 }
 
+// ---- file ingest ---------------------------------------------------------------------------
+
+int ktri_binary_file_shape(const char* stem, uint64_t* n_out, uint64_t* nnz_out) {
+    if (!stem || !n_out || !nnz_out) return KTRI_ERR_INVALID_ARGUMENT;
+    struct stat a, b;
+    const std::string s(stem);
+    if (stat((s + ".first_out").c_str(), &a) != 0 || stat((s + ".head").c_str(), &b) != 0) return KTRI_ERR_IO;
+    if (a.st_size < 8 || a.st_size % 8 || b.st_size % 8) return KTRI_ERR_INVALID_CSR;
+    *n_out = (uint64_t)a.st_size / 8 - 1;
+    *nnz_out = (uint64_t)b.st_size / 8;
+    return KTRI_OK;
+}
+
+int ktri_count_binary_file(ktri_ctx* ctx, const char* stem, uint64_t* total_out, uint64_t* per_vertex_out,
+                           const ktri_opts* opts, uint64_t chunk_bytes) {
+    const ktri::Options opt = resolve(opts);
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!stem || !total_out) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "stem and total_out are required");
+    uint64_t n = 0, nnz = 0;
+    int rc = ktri_binary_file_shape(stem, &n, &nnz);
+    if (rc) return set_error(ctx, rc, std::string("cannot read ") + stem + ".first_out / .head");
+    const u64 dummy = 0;
+    rc = check_common(ctx, &dummy, &dummy, n, nnz, total_out, opt);
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    if (chunk_bytes == 0) chunk_bytes = 64ull << 20;
+    chunk_bytes = std::max<u64>(8, chunk_bytes & ~7ull);
+    const std::string s(stem);
+    const int ffo = open((s + ".first_out").c_str(), O_RDONLY);
+    const int fhd = open((s + ".head").c_str(), O_RDONLY);
+    void* pinned[2] = {nullptr, nullptr};
+    cudaEvent_t freed[2] = {nullptr, nullptr};
+    auto cleanup = [&](int code) {
+        if (ffo >= 0) close(ffo);
+        if (fhd >= 0) close(fhd);
+        for (int i = 0; i < 2; ++i) {
+            if (freed[i]) {
+                cudaEventSynchronize(freed[i]);
+                cudaEventDestroy(freed[i]);
+            }
+            if (pinned[i]) cudaFreeHost(pinned[i]);
+        }
+        return code;
+    };
+    if (ffo < 0 || fhd < 0) return cleanup(set_error(ctx, KTRI_ERR_IO, "cannot open the graph files"));
+    if (n == 0) {
+        *total_out = 0;
+        return cleanup(nnz ? set_error(ctx, KTRI_ERR_INVALID_CSR, "edges without vertices") : KTRI_OK);
+    }
+    Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide, opt.small_outdegree,
+                           opt.segment);
+    // two device staging chunks for u64 ids follow the count's workspace
+    const size_t x_stage = L.bytes;
+    L.bytes = align_up(x_stage + 2 * chunk_bytes);
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return cleanup(rc);
+    for (int i = 0; i < 2; ++i) {
+        if (cudaHostAlloc(&pinned[i], chunk_bytes, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&freed[i], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return cleanup(set_error(ctx, KTRI_ERR_OUT_OF_MEMORY, "pinned staging buffers"));
+        }
+    }
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    char* stage = base + x_stage;
+    cudaStream_t st = ctx->stream;
+    // file -> pinned chunk (read on the host) -> device, two chunks in flight: the read of one
+    // chunk overlaps the copy (and id narrowing) of the other
+    int slot = 0;
+    u64 fo_first = 1, fo_last = 0;
+    auto pump = [&](int fd, u64 bytes, char* dst, bool narrow) -> int {
+        for (u64 off = 0; off < bytes; off += chunk_bytes) {
+            const u64 len = std::min<u64>(chunk_bytes, bytes - off);
+            KTRI_CK(ctx, cudaEventSynchronize(freed[slot]));
+            u64 got = 0;
+            while (got < len) {
+                const ssize_t r = pread(fd, static_cast<char*>(pinned[slot]) + got, len - got, (off_t)(off + got));
+                if (r <= 0) return set_error(ctx, KTRI_ERR_IO, "short read of the graph files");
+                got += (u64)r;
+            }
+            if (!narrow) {
+                if (off == 0) fo_first = *static_cast<const u64*>(pinned[slot]);
+                if (off + len == bytes)
+                    fo_last = *reinterpret_cast<const u64*>(static_cast<const char*>(pinned[slot]) + len - 8);
+                KTRI_CK(ctx, cudaMemcpyAsync(dst + off, pinned[slot], len, cudaMemcpyHostToDevice, st));
+            } else {
+                char* sdev = stage + (size_t)slot * chunk_bytes;
+                KTRI_CK(ctx, cudaMemcpyAsync(sdev, pinned[slot], len, cudaMemcpyHostToDevice, st));
+                ktri::launch_narrow_ids(reinterpret_cast<const u64*>(sdev), len / 8,
+                                        reinterpret_cast<u32*>(dst) + off / 8, ctx->num_sms, st);
+            }
+            KTRI_CK(ctx, cudaEventRecord(freed[slot], st));
+            slot ^= 1;
+        }
+        return KTRI_OK;
+    };
+    rc = pump(ffo, 8 * (n + 1), reinterpret_cast<char*>(d_fo), false);
+    if (rc) return cleanup(rc);
+    if (fo_first != 0 || fo_last != nnz)
+        return cleanup(set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz"));
+    rc = pump(fhd, 8 * nnz, reinterpret_cast<char*>(d_head), true);
+    if (rc) return cleanup(rc);
+    KTRI_CK(ctx, cudaGetLastError());
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false);
+    if (rc) return cleanup(rc);
+    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
+    if (per_vertex_out)
+        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
+    return cleanup(rc);
+}
+
+// ---- triangle listing (checking) -----------------------------------------------------------
+
+int ktri_list_triangles(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                        uint32_t* triples_out, uint64_t capacity, uint64_t* count_out) {
+    ktri::Options opt;
+    opt.method = KTRI_METHOD_MERGE;
+    int rc = check_common(ctx, first_out, head, n, nnz, count_out, opt);
+    if (rc) return rc;
+    if (capacity && !triples_out) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "triples_out is NULL");
+    if (capacity > (1ull << 40)) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "capacity above 2^40 triangles");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    *count_out = 0;
+    if (n == 0) return KTRI_OK;
+    if (first_out[0] != 0 || first_out[n] != nnz)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
+    Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true);
+    const size_t x_tri = L.bytes, x_pos = align_up(x_tri + sizeof(u32) * 3 * capacity);
+    L.bytes = align_up(x_pos + sizeof(u64));
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
+    auto* d_total = reinterpret_cast<u64*>(base + L.total);
+    ktri::TriangleSink sink;
+    sink.triples = reinterpret_cast<u32*>(base + x_tri);
+    sink.cap = capacity;
+    sink.pos = reinterpret_cast<unsigned long long*>(base + x_pos);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemsetAsync(sink.pos, 0, sizeof(u64), st));
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz, cudaMemcpyHostToDevice, st));
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false, sink)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false, sink);
+    if (rc) return rc;
+    u64 total = 0;
+    KTRI_CK(ctx, cudaMemcpyAsync(&total, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc) return rc;
+    const u64 got = total < capacity ? total : capacity;
+    if (got) KTRI_CK(ctx, cudaMemcpy(triples_out, sink.triples, sizeof(u32) * 3 * got, cudaMemcpyDeviceToHost));
+    *count_out = total;
+    ctx->stats.triangles = total;
+    return total > capacity ? set_error(ctx, KTRI_ERR_OUT_OF_MEMORY, "more triangles than the output capacity")
+                            : KTRI_OK;
+}
+
 // ---- oriented lists (the katric local phase) ---------------------------------------------
 
 int ktri_count_dag_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t m,
@@ -619,21 +792,18 @@ int ktri_count_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
             return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out is not monotone");
     if (m > (1ull << 62)) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "too many edges");
     const u64 nnz = 2 * m;
-    const Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide, opt.small_outdegree,
-                                 opt.segment);
+    Layout L = make_layout(n, nnz, opt.method, ctx->num_sms, true, true, opt.force_wide, opt.small_outdegree,
+                           opt.segment);
+    // the caller's lists and the scan sums follow the count's workspace
+    const size_t x_fo = L.bytes, x_head = align_up(x_fo + sizeof(u64) * (n + 1)),
+                 x_sums = align_up(x_head + sizeof(u32) * m);
+    L.bytes = align_up(x_sums + sizeof(u64) * (ktri::dag_scan_chunks(n) + 1));
     rc = ensure_ws(ctx, L.bytes);
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->ws);
-    // the caller's lists, the in-list cursors and the scan sums sit in the out-list region
-    // (at least 4 (2m + 3n + 8) bytes) until orientation overwrites it
-    char* scratch = base + L.headp;
-    auto* dfo = reinterpret_cast<u64*>(scratch);
-    const size_t off_head = align_up(sizeof(u64) * (n + 1));
-    auto* dhead = reinterpret_cast<u32*>(scratch + off_head);
-    auto* sums = reinterpret_cast<u64*>(scratch + align_up(off_head + sizeof(u32) * m));
-    if (align_up(off_head + sizeof(u32) * m) + sizeof(u64) * (ktri::dag_scan_chunks(n) + 1) >
-        sizeof(u32) * ktri::oriented_capacity(n, nnz))
-        return set_error(ctx, KTRI_ERR_UNSUPPORTED, "workspace layout too small for the oriented lists");
+    auto* dfo = reinterpret_cast<u64*>(base + x_fo);
+    auto* dhead = reinterpret_cast<u32*>(base + x_head);
+    auto* sums = reinterpret_cast<u64*>(base + x_sums);
     auto* fs = reinterpret_cast<u64*>(base + L.in_fo);
     auto* hs = reinterpret_cast<u32*>(base + L.in_head);
     auto* cursor = reinterpret_cast<u32*>(base + L.deg);

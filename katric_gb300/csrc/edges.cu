@@ -289,7 +289,8 @@ template <typename OffT>
 __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<OffT>* __restrict__ vdesc,
                                                             const u32* __restrict__ headp, int method, u64 cutoff,
                                                             double hybrid_scale, u64* __restrict__ cnt,
-                                                            u64* __restrict__ partials, Control* ctl) {
+                                                            u64* __restrict__ partials, Control* ctl,
+                                                            TriangleSink sink) {
     __shared__ u64 s_red[EDGE_BLOCK / 32];
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
@@ -305,12 +306,15 @@ __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<Of
             const Desc<OffT> dv = load_desc(vdesc + v);
             const u32* A = headp + (u64)dv.start;
             u64 tv = 0;
-            auto hit_w = [&](u32 w, u32) { atomicAdd(&cnt[w], 1ull); };
             if (method == KTRI_METHOD_BINARY) {
                 for (u32 k0 = 0; k0 < dv.d; k0 += 32) {
                     u32 c = 0, u = 0;
                     if (k0 + lane < dv.d) {
                         u = __ldg(A + k0 + lane);
+                        auto hit_w = [&](u32 w, u32) {
+                            atomicAdd(&cnt[w], 1ull);
+                            sink.emit((u32)v, u, w);
+                        };
                         const Desc<OffT> du = load_desc(vdesc + u);
                         c = lane_binary(A, dv.d, headp + (u64)du.start, du.d, cutoff, hit_w, &overflow);
                         if (c) atomicAdd(&cnt[u], (u64)c);
@@ -323,6 +327,10 @@ __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<Of
             } else {
                 for (u32 k = 0; k < dv.d; ++k) {
                     const u32 u = __ldg(A + k);
+                    auto hit_w = [&](u32 w, u32) {
+                        atomicAdd(&cnt[w], 1ull);
+                        sink.emit((u32)v, u, w);
+                    };
                     const Desc<OffT> du = load_desc(vdesc + u);
                     const u32* B = headp + (u64)du.start;
                     u32 c;
@@ -449,9 +457,9 @@ int count_grid_edges(int num_sms) { return num_sms * 8; }
 
 template <typename OffT>
 void launch_count_edges(u64 n, const void* vdesc, const u32* headp, int method, u64 cutoff, double hybrid_scale,
-                        u64* cnt, u64* partials, int grid, Control* ctl, cudaStream_t st) {
+                        u64* cnt, u64* partials, int grid, Control* ctl, TriangleSink sink, cudaStream_t st) {
     k_count_edges<OffT><<<grid, EDGE_BLOCK, 0, st>>>(n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp, method,
-                                                     cutoff, hybrid_scale, cnt, partials, ctl);
+                                                     cutoff, hybrid_scale, cnt, partials, ctl, sink);
 }
 
 template <typename OffT>
@@ -482,7 +490,7 @@ void launch_intersect_pairs(int method, const u32* a_vals, const u64* a_off, con
     template void launch_sort_lists<OffT>(u64, const void*, u32*, u32*, u32*, u32*, u64, int, Control*, int,       \
                                           cudaStream_t);                                                            \
     template void launch_count_edges<OffT>(u64, const void*, const u32*, int, u64, double, u64*, u64*, int,         \
-                                           Control*, cudaStream_t);                                                 \
+                                           Control*, TriangleSink, cudaStream_t);                                   \
     template void launch_outdeg<OffT>(u64, const void*, u64*, int, cudaStream_t);                                  \
     template void launch_export<OffT>(u64, const void*, const u32*, const u64*, u32*, int, cudaStream_t);
 KTRI_INST(u32)

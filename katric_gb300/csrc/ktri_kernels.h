@@ -41,6 +41,36 @@ inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d, u32 seg) {
     return owners + nnz / seg + 1;
 }
 
+// Optional list of the triangles found by the edge-iterator kernel (debug listing): each
+// triangle (v, u, w) is written, ids in increasing order, at the next position below cap.
+struct TriangleSink {
+    uint32_t* triples = nullptr;  // 3 * cap ids
+    u64 cap = 0;
+    unsigned long long* pos = nullptr;
+#ifdef __CUDACC__
+    __device__ __forceinline__ void emit(uint32_t a, uint32_t b, uint32_t c) const {
+        if (!triples) return;
+        const u64 p = atomicAdd(pos, 1ull);
+        if (p >= cap) return;
+        uint32_t x = a < b ? a : b, y = a < b ? b : a;
+        uint32_t z = c;
+        if (z < y) {
+            const uint32_t t = y;
+            y = z;
+            z = t;
+        }
+        if (y < x) {
+            const uint32_t t = x;
+            x = y;
+            y = t;
+        }
+        triples[3 * p] = x;
+        triples[3 * p + 1] = y;
+        triples[3 * p + 2] = z;
+    }
+#endif
+};
+
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
                  int num_sms, cudaStream_t st);
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
@@ -67,6 +97,9 @@ cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, co
                               cudaEvent_t after_small, cudaEvent_t after_large);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
 
+// u64 ids (the binary file format) -> u32 ids; ids above 2^32 - 1 become 0xFFFFFFFF.
+void launch_narrow_ids(const u64* src, u64 count, u32* dst, int num_sms, cudaStream_t st);
+
 // Oriented out-lists -> undirected CSR of their edges (fs: n + 1 offsets, hs: 2m ids).  cursor
 // needs n u32 and sums dag_scan_chunks(n) u64 of scratch.
 u64 dag_scan_chunks(u64 n);
@@ -88,7 +121,7 @@ void launch_sort_lists(u64 n, const void* vdesc, u32* headp, u32* mid_list, u32*
                        u64 scratch_per_block, int big_grid, Control* ctl, int num_sms, cudaStream_t st);
 template <typename OffT>
 void launch_count_edges(u64 n, const void* vdesc, const u32* headp, int method, u64 cutoff, double hybrid_scale,
-                        u64* cnt, u64* partials, int grid, Control* ctl, cudaStream_t st);
+                        u64* cnt, u64* partials, int grid, Control* ctl, TriangleSink sink, cudaStream_t st);
 int count_grid_edges(int num_sms);
 
 // Oriented CSR export: compact copy of the out-lists (after sorting).

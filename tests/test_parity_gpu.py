@@ -230,3 +230,60 @@ def test_intersection_random_gpu(counter, method):
     got = counter.intersect_pairs(pairs, method=method)
     for (a, b), g in zip(pairs, got):
         assert sorted(g) == np.intersect1d(a, b).tolist()
+
+
+@pytest.mark.parametrize("gen", ["rmat", "gnm", "clique"])
+def test_list_triangles_no_duplicates(counter, oracle, gen):
+    """The debug check of run_shmem (shared_memory_cetric.h:151-167): every emitted triangle,
+    sorted, has no duplicate; here also every row is a triangle and the rows number the total."""
+    if gen == "clique":
+        fo, hd = csr_from_edges(40, [(i, j) for i in range(40) for j in range(i + 1, 40)])
+    else:
+        g = Graph.rmat(10, 16, seed=3) if gen == "rmat" else Graph.gnm(2000, 12000, seed=4)
+        fo, hd = g.first_out, g.head
+    total = oracle.count(fo, hd, num_threads=4)[0]
+    tri = counter.list_triangles(fo, hd)
+    assert len(tri) == total
+    assert np.all(tri[:, 0] < tri[:, 1]) and np.all(tri[:, 1] < tri[:, 2])
+    keys = (tri[:, 0].astype(np.uint64) << np.uint64(42)) | (tri[:, 1].astype(np.uint64) << np.uint64(21)) | \
+        tri[:, 2].astype(np.uint64)
+    assert len(np.unique(keys)) == len(keys)
+    n = len(fo) - 1
+    adj = set()
+    f = fo.astype(np.int64)
+    for v in range(n):
+        for u in hd[f[v]:f[v + 1]]:
+            adj.add((v, int(u)))
+    for x, y, z in tri[:2000].tolist():
+        assert (x, y) in adj and (y, z) in adj and (x, z) in adj
+    with pytest.raises(KtriError) as e:
+        counter.list_triangles(fo, hd, capacity=max(0, total - 1))
+    assert e.value.code == _native.ERR_OUT_OF_MEMORY
+
+
+@pytest.mark.parametrize("chunk", [0, 4096, 8 * 1000 + 8])
+def test_count_binary_file_overlapped_ingest(counter, oracle, tmp_path, chunk):
+    """Counting straight from the reference's binary format (u64 .first_out / .head), the file
+    read in chunks overlapping the host-to-device copies."""
+    g = Graph.rmat(13, 16, seed=11)
+    stem = str(tmp_path / "g")
+    g.write_binary(stem)
+    want_t, want_pv, _ = oracle.count(g.first_out, g.head, num_threads=8)
+    t, pv = counter.count_binary_file(stem, chunk_bytes=chunk)
+    assert t == want_t and np.array_equal(pv, want_pv)
+
+
+def test_count_binary_file_errors(counter, tmp_path):
+    with pytest.raises(KtriError) as e:
+        counter.count_binary_file(str(tmp_path / "missing"))
+    assert e.value.code == _native.ERR_IO
+    stem = str(tmp_path / "bad")
+    np.array([0, 2, 3, 3], np.uint64).tofile(stem + ".first_out")
+    np.array([1, 7, 0], np.uint64).tofile(stem + ".head")  # id 7 >= n
+    with pytest.raises(KtriError) as e:
+        counter.count_binary_file(stem)
+    assert e.value.code == _native.ERR_INVALID_CSR
+    np.array([0, 2, 3, 4], np.uint64).tofile(stem + ".first_out")  # first_out[n] != nnz
+    with pytest.raises(KtriError) as e:
+        counter.count_binary_file(stem)
+    assert e.value.code == _native.ERR_INVALID_CSR
