@@ -46,7 +46,7 @@ WORKLOADS = {
                   repeat=0.3, budget=120 << 30, seed=5),
 }
 METRIC = "edges/s (undirected edges / time of one exact total + per-vertex count)"
-KERNELS_PER_STEP = 6  # k_prep, k_orient, k_desc, k_count_small, k_count_large, k_final
+KERNELS_PER_STEP = 7  # k_prep, k_orient, k_desc, k_count_small, k_count_medium, k_count_large, k_final
 
 
 def make_graph(name: str):
@@ -120,6 +120,20 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_traffic(workload: str):
+    """DRAM bytes (read + write) of the intersection-phase kernels of one count, from the ncu
+    capture summarised in profiles/dram_traffic.txt (None when that workload was not captured)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if parts and not line.startswith("#") and parts[0] == workload:
+                return float(parts[1])
+    return None
 
 
 def peaks():
@@ -280,7 +294,7 @@ def run_batch(args):
         "batched_vs_plain": plain_ms / ms,
         "autotune": tune,
         "triangles_total": int(ref_tot.sum().item()),
-        "gpu_launches": 9 * args.steps,
+        "gpu_launches": (KERNELS_PER_STEP + 1) * args.steps,  # the pipeline's kernels + k_graph_totals per replay
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -542,13 +556,16 @@ def main():
         "triangles": total_ref,
         "hbm_gbs_algorithmic": b_total / (ms / 1e3) / 1e9,
         "phases_ms": {"orient": statistics.mean(orient_ms), "count_small": statistics.mean(small_ms),
-                      "count_large": statistics.mean(large_ms), "count_total": k_ms},
+                      "count_medium_large": statistics.mean(large_ms), "count_total": k_ms},
         "work": {"wedge_checks": wedge_checks, "oriented_edges": m_oriented, "streamed_entries": streamed},
-        "roofline": {"bound": "hbm", "kernel": "intersection phase (k_count_small + k_count_large + k_final)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "intersection phase (k_count_small + k_count_medium + k_count_large + k_final)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
-                     "algorithmic_bytes": b_int, "traffic": None},
+                     "algorithmic_bytes": b_int, "traffic": measured_traffic(args.workload),
+                     "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum of the three counting kernels, one capture)"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8)},
         "gpu_launches": KERNELS_PER_STEP * args.steps,

@@ -34,19 +34,44 @@ namespace ktri {
 
 constexpr size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Hit counters of the owners' tables are 16-bit, two per word: a key gets at most one hit per
+// streamed list, and a tile streams at most LARGE_SEG (block and warp kernels) or one tile's
+// slots (small-owner kernel) lists, so they cannot overflow.
+__device__ __forceinline__ void hit16(u32* hits32, u32 slot) { atomicAdd(&hits32[slot >> 1], 1u << ((slot & 1u) << 4)); }
+__device__ __forceinline__ u32 read16(const u32* hits32, u32 slot) { return (hits32[slot >> 1] >> ((slot & 1u) << 4)) & 0xFFFFu; }
+
+// Lookup with a 16-bit hit counter (same table layout as bucket_probe).
+__device__ __forceinline__ u32 bucket_probe16(const u32* keys, u32* hits32, u32 lg, u32 w) {
+    const u32 nb_mask = (1u << (lg - 2)) - 1;
+    u32 b = bucket_home(w, lg);
+    for (u32 it = 0; it <= nb_mask; ++it) {
+        const uint4 q = *reinterpret_cast<const uint4*>(keys + 4 * b);
+        const bool m0 = q.x == w, m1 = q.y == w, m2 = q.z == w, m3 = q.w == w;
+        if (m0 | m1 | m2 | m3) {
+            hit16(hits32, 4 * b + (m0 ? 0u : (m1 ? 1u : (m2 ? 2u : 3u))));
+            return 1u;
+        }
+        if (q.w == EMPTY_KEY) return 0u;
+        b = (b + 1) & nb_mask;
+    }
+    return 0u;
+}
+
+
 template <int BLOCK, int IPT, int SD, typename OffT>
 struct SmallLayout {
     static constexpr int TILE = BLOCK * IPT;
     static constexpr int TBL = 4 * (TILE + 2 * SD);  // sum of per-owner table sizes (pow2 >= max(4, 2d) <= 4d)
     static constexpr int WPT = (TILE + 1 + BLOCK - 1) / BLOCK;
+    static_assert(TILE < 65536, "window offsets and hit counters are 16-bit");
     static constexpr size_t off_fo = 0;  // first_out of the window, clamped to the tile, relative to its first slot
-    static constexpr size_t off_desc = align16(off_fo + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_desc = align16(off_fo + sizeof(unsigned short) * (TILE + 2));
     static constexpr size_t off_tb = align16(off_desc + sizeof(Desc<OffT>) * (TILE + 2));
+    // key offsets of the owners while the tables are filled, then the owners' hit totals
     static constexpr size_t off_ko = align16(off_tb + sizeof(u32) * (TILE + 2));
-    static constexpr size_t off_own = align16(off_ko + sizeof(u32) * (TILE + 2));
-    static constexpr size_t off_keys = align16(off_own + sizeof(u32) * (TILE + 2));
-    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TBL);
-    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * TBL);
+    static constexpr size_t off_keys = align16(off_ko + sizeof(u32) * (TILE + 2));
+    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TBL);  // two u16 counters per word
+    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * (TBL / 2));
     static constexpr size_t off_qs = align16(off_qy + sizeof(u32) * TILE);
     static constexpr size_t off_qm = align16(off_qs + sizeof(OffT) * TILE);
     static constexpr size_t off_ord = align16(off_qm + sizeof(u32) * TILE);
@@ -66,11 +91,11 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
     constexpr int WPT = L::WPT;
     static_assert(SD < 64, "list length is packed in 6 bits");
     extern __shared__ __align__(16) unsigned char smem[];
-    u32* s_fo = reinterpret_cast<u32*>(smem + L::off_fo);
+    unsigned short* s_fo = reinterpret_cast<unsigned short*>(smem + L::off_fo);
     Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
     u32* s_tb = reinterpret_cast<u32*>(smem + L::off_tb);
     u32* s_ko = reinterpret_cast<u32*>(smem + L::off_ko);
-    u32* s_own = reinterpret_cast<u32*>(smem + L::off_own);
+    u32* s_own = reinterpret_cast<u32*>(smem + L::off_ko);  // after the tables are filled
     u32* s_keys = reinterpret_cast<u32*>(smem + L::off_keys);
     u32* s_hits = reinterpret_cast<u32*>(smem + L::off_hits);
     u32* q_y = reinterpret_cast<u32*>(smem + L::off_qy);
@@ -92,19 +117,21 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
     u32 dup = 0;
 
     while (true) {
-        if (threadIdx.x == 0) s_b[2] = atomicAdd(&ctl->small_next, 1ull);
+        if (threadIdx.x == 0) {
+            const u64 t = atomicAdd(&ctl->small_next, 1ull);
+            s_b[2] = t;
+            if (t < ntiles) {
+                s_b[0] = tile_i0[t];
+                s_b[1] = tile_i0[t + 1];
+            }
+            s_qn = 0;
+        }
         if (threadIdx.x < SD + 2) s_bins[threadIdx.x] = 0;
-        if (threadIdx.x == 0) s_qn = 0;
         __syncthreads();
         const u64 tile = s_b[2];
         if (tile >= ntiles) break;
         const u64 d0 = tile * TILE;
         const u64 d1 = d0 + TILE < total_items ? d0 + TILE : total_items;
-        if (threadIdx.x == 0) {
-            s_b[0] = tile_i0[tile];
-            s_b[1] = tile_i0[tile + 1];
-        }
-        __syncthreads();
         const u64 i0 = s_b[0], i1 = s_b[1];
         if (i0 >= n) {  // only trailing vertex-end events: nothing to count
             __syncthreads();
@@ -116,11 +143,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         for (u32 k = threadIdx.x; k <= nw; k += BLOCK) {
             u64 f = fo[i0 + k];
             f = f < j0 ? j0 : (f > j1 ? j1 : f);
-            s_fo[k] = (u32)(f - j0);
+            s_fo[k] = (unsigned short)(f - j0);
         }
         for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
             s_desc[k] = load_desc(vdesc + i0 + k);
-            s_own[k] = 0;
         }
         __syncthreads();
 
@@ -160,10 +186,8 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         }
         const u32 table_slots = ptot >> 16, nkeys = ptot & 0xFFFFu;
         if (threadIdx.x == 0) s_ko[nw] = nkeys;
-        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
-            s_keys[s] = EMPTY_KEY;
-            s_hits[s] = 0;
-        }
+        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) s_keys[s] = EMPTY_KEY;
+        for (u32 s = threadIdx.x; s < table_slots / 2; s += BLOCK) s_hits[s] = 0;
         __syncthreads();
 
         // insert the out-lists of the owners (one key per thread per step)
@@ -243,7 +267,9 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         }
         __syncthreads();
 
-        // counting sort of the queue by list length
+        // counting sort of the queue by list length; the key offsets are no longer needed and
+        // their words become the owners' hit totals
+        for (u32 k = threadIdx.x; k < nw; k += BLOCK) s_own[k] = 0;
         const u32 qn = s_qn;
         if (threadIdx.x < 32) {
             u32 c0 = s_bins[lane], c1 = lane + 32 < SD + 2 ? s_bins[lane + 32] : 0;
@@ -277,7 +303,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             const u32 o = meta >> 6, dy = meta & 63u;
             const u32 tb = s_tb[o];
             const u32* keys = s_keys + (tb >> 5);
-            u32* hitc = s_hits + (tb >> 5);
+            u32* hitc = s_hits + ((tb >> 5) >> 1);  // table offsets are multiples of 4 slots
             const u32 lg = tb & 31u;
             const u64 q0 = (u64)q_s[qi] >> 2;
             u32 hits = 0;
@@ -285,10 +311,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             for (int c = 0; c < SD / 4; ++c) {
                 if (4 * c < (int)dy) {
                     const uint4 qv = __ldg(headp4 + q0 + c);
-                    hits += bucket_probe(keys, hitc, lg, qv.x);
-                    if (4 * c + 1 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.y);
-                    if (4 * c + 2 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.z);
-                    if (4 * c + 3 < (int)dy) hits += bucket_probe(keys, hitc, lg, qv.w);
+                    hits += bucket_probe16(keys, hitc, lg, qv.x);
+                    if (4 * c + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.y);
+                    if (4 * c + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.z);
+                    if (4 * c + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.w);
                 }
             }
             if (hits) {
@@ -300,7 +326,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
 
         // flush: hits of every key (vertex w), then the owners' own counts
         for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
-            const u32 h = s_hits[s];
+            const u32 h = read16(s_hits, s);
             if (h) atomicAdd(&cnt[s_keys[s]], (u64)h);
         }
         for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
@@ -330,28 +356,6 @@ struct LargeLayout {
     static constexpr size_t off_qd = align16(off_qy + sizeof(u32) * LARGE_SEG);
     static constexpr size_t bytes = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
 };
-
-// Hit counters of the large owners' tables are 16-bit, two per word: a key gets at most one
-// hit per streamed list and a tile streams at most LARGE_SEG lists, so they cannot overflow.
-__device__ __forceinline__ void hit16(u32* hits32, u32 slot) { atomicAdd(&hits32[slot >> 1], 1u << ((slot & 1u) << 4)); }
-__device__ __forceinline__ u32 read16(const u32* hits32, u32 slot) { return (hits32[slot >> 1] >> ((slot & 1u) << 4)) & 0xFFFFu; }
-
-// Lookup with a 16-bit hit counter (same table layout as bucket_probe).
-__device__ __forceinline__ u32 bucket_probe16(const u32* keys, u32* hits32, u32 lg, u32 w) {
-    const u32 nb_mask = (1u << (lg - 2)) - 1;
-    u32 b = bucket_home(w, lg);
-    for (u32 it = 0; it <= nb_mask; ++it) {
-        const uint4 q = *reinterpret_cast<const uint4*>(keys + 4 * b);
-        const bool m0 = q.x == w, m1 = q.y == w, m2 = q.z == w, m3 = q.w == w;
-        if (m0 | m1 | m2 | m3) {
-            hit16(hits32, 4 * b + (m0 ? 0u : (m1 ? 1u : (m2 ? 2u : 3u))));
-            return 1u;
-        }
-        if (q.w == EMPTY_KEY) return 0u;
-        b = (b + 1) & nb_mask;
-    }
-    return 0u;
-}
 
 // One-hash membership filter of the owner's keys (2^fl bits): a clear bit is a sure miss.
 __device__ __forceinline__ u32 filter_bit(u32 w, u32 fl) { return (w * 0x85EBCA6Bu) >> (32 - fl); }
@@ -575,7 +579,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
 template <int BLOCK>
 struct MediumLayout {
     static constexpr int NW = BLOCK / 32;
-    static constexpr int TS = 4 * MEDIUM_D;  // table slots per warp (at most a quarter full)
+    static constexpr int TS = 2 * MEDIUM_D;  // table slots per warp (a quarter to half full)
     static constexpr int FW = MEDIUM_D / 2;  // filter words per warp (16 bits per key)
     static constexpr int WBUF = 64;
     static constexpr int PER_WARP = TS + TS / 2 + FW + WBUF;  // u32 words: keys, 16-bit hits, filter, buffer
@@ -589,7 +593,7 @@ __global__ void __launch_bounds__(BLOCK)
                    const uint2* __restrict__ mtiles, u32 seg, u64* __restrict__ cnt,
                    u64* __restrict__ partials, Control* ctl) {
     using L = MediumLayout<BLOCK>;
-    constexpr int U = 8;
+    constexpr int U = 4;  // medium owners' streamed lists are shorter than 256 entries
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ u64 s_red[L::NW];
     if (ctl->err & DEV_ERR_MASK) return;
