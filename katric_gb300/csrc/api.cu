@@ -303,6 +303,8 @@ int device_status(ktri_ctx* ctx) {
         }
     }
     const u32 e = h.err & ktri::DEV_ERR_MASK;
+    if (e & ktri::DEV_ERR_TIMEOUT)
+        return set_error(ctx, KTRI_ERR_TIMEOUT, "a bulk copy into shared memory did not complete in time");
     if (e & ktri::DEV_ERR_DEGREE)
         return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out is not a valid offset array (non-monotone, "
                                                     "first_out[0] != 0, first_out[n] != nnz, or a degree >= 2^32)");
@@ -372,6 +374,7 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
     u32 herr = 0;
     if (cudaMemcpyAsync(&herr, &ctl->err, sizeof(u32), cudaMemcpyDeviceToHost, st) != cudaSuccess) return KTRI_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return KTRI_ERR_CUDA;
+    if (herr & ktri::DEV_ERR_TIMEOUT) return KTRI_ERR_TIMEOUT;
     return (herr & ktri::DEV_ERR_MASK) ? KTRI_ERR_INVALID_CSR : KTRI_OK;
 }
 
@@ -1048,6 +1051,8 @@ int ktri_plan_check(ktri_plan* plan) {
     KTRI_CK(ctx, cudaStreamSynchronize(plan->last));
     u32 err = 0;
     KTRI_CK(ctx, cudaMemcpy(&err, &plan->ctl->err, sizeof(u32), cudaMemcpyDeviceToHost));
+    if (err & ktri::DEV_ERR_TIMEOUT)
+        return set_error(ctx, KTRI_ERR_TIMEOUT, "a bulk copy into shared memory did not complete in time");
     if (err & ktri::DEV_ERR_MASK) return set_error(ctx, KTRI_ERR_INVALID_CSR, "invalid CSR found on the device");
     return KTRI_OK;
 }

@@ -34,6 +34,40 @@ namespace ktri {
 
 constexpr size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Bulk (TMA) copies into shared memory, completed on an mbarrier.  The copy engine moves a
+// 16-byte-aligned run of bytes (a multiple of 16) from global to shared memory and counts the
+// bytes against the barrier's expected transaction count.
+__device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, u32 bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, u32 parity) {
+    u32 ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the barrier's phase of the given parity; gives up after a bounded number of polls
+// (each poll itself blocks for a short hardware-defined time) and reports false.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, u32 parity) {
+    for (u32 it = 0; it < (1u << 22); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 // Hit counters of the owners' tables are 16-bit, two per word: a key gets at most one hit per
 // streamed list, and a tile streams at most LARGE_SEG (block and warp kernels) or one tile's
 // slots (small-owner kernel) lists, so they cannot overflow.
@@ -307,14 +341,25 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             const u32 lg = tb & 31u;
             const u64 q0 = (u64)q_s[qi] >> 2;
             u32 hits = 0;
+            // the list's 16-byte groups are loaded PRE at a time before any probe, so their
+            // latencies overlap instead of adding up
+            constexpr int PRE = 4;
 #pragma unroll
-            for (int c = 0; c < SD / 4; ++c) {
-                if (4 * c < (int)dy) {
-                    const uint4 qv = __ldg(headp4 + q0 + c);
-                    hits += bucket_probe16(keys, hitc, lg, qv.x);
-                    if (4 * c + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.y);
-                    if (4 * c + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.z);
-                    if (4 * c + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv.w);
+            for (int c0 = 0; c0 < SD / 4; c0 += PRE) {
+                if (4 * c0 < (int)dy) {
+                    uint4 qv[PRE];
+#pragma unroll
+                    for (int c = 0; c < PRE; ++c)
+                        qv[c] = 4 * (c0 + c) < (int)dy ? __ldg(headp4 + q0 + c0 + c)
+                                                       : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+#pragma unroll
+                    for (int c = 0; c < PRE; ++c) {
+                        const int e = 4 * (c0 + c);
+                        if (e < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
+                        if (e + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
+                        if (e + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
+                        if (e + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
+                    }
                 }
             }
             if (hits) {
@@ -459,9 +504,18 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     __shared__ u64 s_red[NW];
     __shared__ u64 s_t;
     __shared__ u32 s_qn, s_next;
+    __shared__ __align__(8) unsigned long long s_bar;  // completion of the owner-list bulk copy
 
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+    fence_proxy_async_smem();
+    __syncthreads();
+    u32 phase = 0;
+    bool timed_out = false;
+    // the owner's keys are staged in the queue's descriptor region, which is free until the scan
+    u32* stage = reinterpret_cast<u32*>(smem + L::off_qd);
+    static_assert(sizeof(Desc<OffT>) * LARGE_SEG >= sizeof(u32) * CAP, "staging fits the queue region");
     u32* wbuf = reinterpret_cast<u32*>(smem + L::off_wbuf) + warp * L::WBUF;
     const u32 lt_mask = (1u << lane) - 1;
     const u64 ntiles = *(volatile unsigned long long*)&ctl->large_tiles;
@@ -494,9 +548,23 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 s_qn = 0;
                 s_next = 0;
             }
+            fence_proxy_async_smem();  // earlier generic accesses of the staging region come first
             __syncthreads();
+            // one bulk copy of the chunk's keys (list starts are 16-byte aligned, and the gapped
+            // layout leaves room to round the length up to whole 16-byte groups)
+            if (threadIdx.x == 0) {
+                const u32 bytes = ((klen + 3u) & ~3u) * (u32)sizeof(u32);
+                mbar_expect_tx(&s_bar, bytes);
+                bulk_copy_g2s(stage, headp + (u64)dxd.start + c0, bytes, &s_bar);
+            }
+            const bool arrived = mbar_wait_bounded(&s_bar, phase);
+            if (__syncthreads_or(!arrived)) {  // the same decision in every thread
+                timed_out = true;
+                break;
+            }
+            phase ^= 1u;
             for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
-                const u32 w = __ldg(headp + (u64)dxd.start + c0 + q);
+                const u32 w = stage[q];
                 if (!bucket_insert(keys, lg, w)) dup = 1;
                 const u32 h = filter_bit(w, fl);
                 atomicOr(&filt[h >> 5], 1u << (h & 31u));
@@ -568,8 +636,10 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             atomicAdd(&cnt[x], bt);
             local_total += bt;
         }
+        if (timed_out) break;
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+    if (timed_out) atomicOr(&ctl->err, DEV_ERR_TIMEOUT);
     if (threadIdx.x == 0) partials[blockIdx.x] = local_total;
 }
 

@@ -36,6 +36,7 @@ enum : uint32_t {
     DEV_ERR_SELF_LOOP = 1u << 1,  // head entry == owner
     DEV_ERR_DUPLICATE = 1u << 2,  // a list holds the same id twice
     DEV_ERR_DEGREE = 1u << 3,     // first_out not monotone, or a degree >= 2^32
+    DEV_ERR_TIMEOUT = 1u << 4,    // a bounded wait (bulk-copy barrier) ran out
     DEV_FLAG_UNSORTED = 1u << 8,  // some input list is not strictly increasing (not an error)
 };
 
