@@ -47,7 +47,8 @@ constexpr size_t ALIGN = 256;
 inline size_t align_up(size_t x) { return (x + ALIGN - 1) & ~(ALIGN - 1); }
 
 struct Layout {
-    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, vdesc = 0, headp = 0, ltiles = 0, spanning = 0, partials = 0, cnt = 0,
+    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, vdesc = 0, headp = 0, ltiles = 0, thist = 0, spanning = 0,
+           partials = 0, cnt = 0,
            total = 0, mid = 0, big = 0, scratch = 0, in_fo = 0, in_head = 0, bytes = 0;
     bool wide = false;
     u64 scratch_per_block = 0;
@@ -85,7 +86,9 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
         // medium-owner tiles, then large-owner tiles, each with room for every owner tile
-        L.ltiles = take(sizeof(uint2) * 2 * ktri::large_tile_capacity(n, nnz, small_d, seg));
+        // medium-owner tiles, large-owner tiles, and the large ones reordered
+        L.ltiles = take(sizeof(uint2) * 3 * ktri::large_tile_capacity(n, nnz, small_d, seg));
+        L.thist = take(sizeof(u32) * ktri::tile_order_scratch_words());
         grid = (u32)(sms * 48);  // bound on the small + medium + large persistent grids (occupancy <= 16 each)
     } else {
         L.mid = take(sizeof(u32) * (n + 1));
@@ -201,9 +204,14 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
     auto* mtiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
-    auto* ltiles = autom ? mtiles + ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment) : nullptr;
+    const u64 tcap = ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment);
+    auto* ltiles = autom ? mtiles + tcap : nullptr;
+    auto* lsorted = autom ? ltiles + tcap : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
                             opt.medium_outdegree, opt.segment, ctl, sms, st);
+    if (autom)
+        ktri::launch_order_tiles(fo, head, n, ltiles, opt.segment, reinterpret_cast<u32*>(base + L.thist), lsorted,
+                                 ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -215,7 +223,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, lsorted,
                                                    opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
                                                    events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
         ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);

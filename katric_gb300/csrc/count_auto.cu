@@ -113,7 +113,7 @@ struct SmallLayout {
 };
 
 template <int BLOCK, int IPT, int SD, typename OffT>
-__global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
+__global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
                                                        const u32* __restrict__ headp,
                                                        const u32* __restrict__ tile_i0, u32 sd,
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
     __shared__ u64 s_red[BLOCK / 32];
     __shared__ u64 s_b[3];
     __shared__ u32 s_bins[SD + 2];
-    __shared__ u32 s_qn;
+    __shared__ u32 s_qn, s_chunk;
 
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
                 s_b[1] = tile_i0[t + 1];
             }
             s_qn = 0;
+            s_chunk = 0;
         }
         if (threadIdx.x < SD + 2) s_bins[threadIdx.x] = 0;
         __syncthreads();
@@ -330,9 +331,16 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
         }
         __syncthreads();
 
-        // stream the queued lists (equal lengths side by side)
-        for (u32 r = threadIdx.x; r < qn; r += BLOCK) {
-            const u32 qi = q_ord[r];
+        // stream the queued lists: warps take chunks of 32 from the length-sorted queue, longest
+        // first, so the lanes of a warp carry equal lengths and the warps finish together
+        while (true) {
+            u32 c32 = 0;
+            if (lane == 0) c32 = atomicAdd(&s_chunk, 32u);
+            c32 = __shfl_sync(0xFFFFFFFFu, c32, 0);
+            if (c32 >= qn) break;
+            const u32 r = c32 + lane;
+            if (r >= qn) continue;
+            const u32 qi = q_ord[qn - 1 - r];
             const u32 meta = q_m[qi];
             const u32 o = meta >> 6, dy = meta & 63u;
             const u32 tb = s_tb[o];
@@ -344,22 +352,21 @@ __global__ void __launch_bounds__(BLOCK) k_count_small(const u64* __restrict__ f
             // the list's 16-byte groups are loaded PRE at a time before any probe, so their
             // latencies overlap instead of adding up
             constexpr int PRE = 4;
-#pragma unroll
+#pragma unroll 1
             for (int c0 = 0; c0 < SD / 4; c0 += PRE) {
-                if (4 * c0 < (int)dy) {
-                    uint4 qv[PRE];
+                if (4 * c0 >= (int)dy) break;
+                uint4 qv[PRE];
 #pragma unroll
-                    for (int c = 0; c < PRE; ++c)
-                        qv[c] = 4 * (c0 + c) < (int)dy ? __ldg(headp4 + q0 + c0 + c)
-                                                       : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+                for (int c = 0; c < PRE; ++c)
+                    qv[c] = 4 * (c0 + c) < (int)dy ? __ldg(headp4 + q0 + c0 + c)
+                                                   : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
 #pragma unroll
-                    for (int c = 0; c < PRE; ++c) {
-                        const int e = 4 * (c0 + c);
-                        if (e < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
-                        if (e + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
-                        if (e + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
-                        if (e + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
-                    }
+                for (int c = 0; c < PRE; ++c) {
+                    const int e = 4 * (c0 + c);
+                    if (e < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
+                    if (e + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
+                    if (e + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
+                    if (e + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
                 }
             }
             if (hits) {

@@ -81,6 +81,12 @@ template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
                  u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st);
 
+// Large-owner tiles reordered by the first vertex their segment streams (hist needs
+// tile_order_scratch_words() u32, sorted the same capacity as tiles).
+u64 tile_order_scratch_words();
+void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, u32 seg, u32* hist,
+                        uint2* sorted, Control* ctl, int num_sms, cudaStream_t st);
+
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
 int count_grid_small(int num_sms);

@@ -248,7 +248,72 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
     }
 }
 
+// Large-owner tiles in the order of the first vertex each segment streams (a counting sort
+// on the top id bits).  Input adjacency lists are mostly in id order, so tiles that run at the
+// same time then stream out-lists from the same region of the list array, and the L2 cache
+// serves the repeats.  Counts do not depend on the order.
+constexpr u32 TILE_BUCKETS = 4096;
+
+__global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head,
+                            const uint2* __restrict__ tiles, u32 seg, u32 shift, u32* hist, Control* ctl) {
+    if (ctl->err & DEV_ERR_MASK) return;
+    const u64 nt = *(volatile unsigned long long*)&ctl->large_tiles;
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
+        const uint2 tl = tiles[t];
+        u32 key = __ldg(head + fo[tl.x] + (u64)tl.y * seg) >> shift;
+        if (key >= TILE_BUCKETS) key = TILE_BUCKETS - 1;
+        atomicAdd(&hist[key], 1u);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
+    constexpr int PER = TILE_BUCKETS / 1024;
+    __shared__ u32 s_warp[32];
+    if (ctl->err & DEV_ERR_MASK) return;
+    u32 v[PER], t = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        v[k] = hist[threadIdx.x * PER + k];
+        t += v[k];
+    }
+    u32 total;
+    u32 run = block_exclusive_scan<1024>(t, s_warp, &total);
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        hist[threadIdx.x * PER + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const uint2* __restrict__ tiles,
+                               u32 seg, u32 shift, u32* cursor, uint2* __restrict__ sorted, Control* ctl) {
+    if (ctl->err & DEV_ERR_MASK) return;
+    const u64 nt = *(volatile unsigned long long*)&ctl->large_tiles;
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
+        const uint2 tl = tiles[t];
+        u32 key = __ldg(head + fo[tl.x] + (u64)tl.y * seg) >> shift;
+        if (key >= TILE_BUCKETS) key = TILE_BUCKETS - 1;
+        sorted[atomicAdd(&cursor[key], 1u)] = tl;
+    }
+}
+
 // ---- launchers ------------------------------------------------------------------------
+
+u64 tile_order_scratch_words() { return TILE_BUCKETS; }
+
+void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, u32 seg, u32* hist,
+                        uint2* sorted, Control* ctl, int num_sms, cudaStream_t st) {
+    if (n == 0) return;
+    u32 bits = 0;
+    while ((1ull << bits) < n) ++bits;
+    const u32 shift = bits > 12 ? bits - 12 : 0;
+    cudaMemsetAsync(hist, 0, sizeof(u32) * TILE_BUCKETS, st);
+    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, seg, shift, hist, ctl);
+    k_tile_scan<<<1, 1024, 0, st>>>(hist, ctl);
+    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, seg, shift, hist, sorted, ctl);
+}
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
                  int num_sms, cudaStream_t st) {
