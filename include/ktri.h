@@ -206,6 +206,20 @@ int ktri_count_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
 int ktri_count_dag_device(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n, uint64_t m,
                           uint64_t* d_total, uint64_t* d_per_vertex, const ktri_opts* opts, void* stream);
 
+/* ---- contraction after the local phase ---------------------------------------------------
+ * CeTriC-X contracts each rank's graph once its local phase is done (cetric.h:872-930):
+ * remove_internal_edges keeps, per local vertex, only its out-edges to other ranks and drops
+ * its in-edges (distributed_graph.h:680-764); compact drops the vertices left without edges and
+ * renumbers the rest (:979-1056); the lists are then sorted by id.  ktri_contract_dag_ctx does
+ * this on the device for lists numbered as ktri_count_dag's input: vertices 0..n_local-1 are
+ * the rank's own, n_local..n-1 its ghosts.  Outputs (caller-sized: kept_out n_local entries,
+ * out_first_out n_local + 1, out_head m): kept_out[k] = the list index of the k-th surviving
+ * vertex, out_first_out / out_head its ghost out-neighbours sorted by id, *kept_count and
+ * *edge_count the sizes. */
+int ktri_contract_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t n_local,
+                          uint64_t m, uint32_t* kept_out, uint64_t* out_first_out, uint32_t* out_head,
+                          uint64_t* kept_count, uint64_t* edge_count);
+
 /* ---- autotuning ---------------------------------------------------------------------------
  * No counterpart in the reference (its strategy is a command-line choice, --intersection-method,
  * apps/parse_parameters.h:156-158).  ktri_autotune times candidate configurations of one count

@@ -205,6 +205,23 @@ class TriangleCounter:
                                                ctypes.byref(opts)))
         return int(total.value), (pv[:n] if pv is not None else None)
 
+    def contract_dag(self, first_out, head, n_local: int):
+        """The contraction that follows the local phase (remove_internal_edges + compact +
+        id sort, cetric.h:872-930) on lists numbered like count_dag's input (vertices
+        0..n_local-1 local, the rest ghosts).  Returns (kept, first_out, head): the surviving
+        local vertices and their ghost out-neighbours sorted by id."""
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, m = len(fo) - 1, len(hd)
+        kept = np.zeros(max(1, n_local), dtype=np.uint32)
+        ofo = np.zeros(n_local + 1, dtype=np.uint64)
+        oh = np.zeros(max(1, m), dtype=np.uint32)
+        k, e = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._check(self._L.ktri_contract_dag_ctx(self._ctx, fo.ctypes.data, hd.ctypes.data if m else None, n, n_local,
+                                                  m, kept.ctypes.data, ofo.ctypes.data, oh.ctypes.data,
+                                                  ctypes.byref(k), ctypes.byref(e)))
+        return kept[: k.value].copy(), ofo[: k.value + 1].copy(), oh[: e.value].copy()
+
     def count_dag_device(self, first_out_ptr: int, head_ptr: int, n: int, m: int, total_ptr: int,
                          per_vertex_ptr: int | None = None, conf: Config | None = None, stream: int = 0) -> None:
         conf = conf or Config()

@@ -85,7 +85,6 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     L.tile_i0 = take(sizeof(u32) * (ktri::base_tiles(n, nnz) + 2));
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
-        // medium-owner tiles, then large-owner tiles, each with room for every owner tile
         // medium-owner tiles, large-owner tiles, and the large ones reordered
         L.ltiles = take(sizeof(uint2) * 3 * ktri::large_tile_capacity(n, nnz, small_d, seg));
         L.thist = take(sizeof(u32) * ktri::tile_order_scratch_words());
@@ -696,6 +695,88 @@ int ktri_count_binary_file(ktri_ctx* ctx, const char* stem, uint64_t* total_out,
     rc = device_status(ctx);
     if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
     return cleanup(rc);
+}
+
+// ---- contraction after the local phase -------------------------------------------------------
+
+int ktri_contract_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t n_local,
+                          uint64_t m, uint32_t* kept_out, uint64_t* out_first_out, uint32_t* out_head,
+                          uint64_t* kept_count, uint64_t* edge_count) {
+    if (!ctx) return KTRI_ERR_INVALID_ARGUMENT;
+    if (!first_out || (m && !head) || !kept_count || !edge_count || !out_first_out || (n_local && !kept_out) ||
+        (m && !out_head))
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "NULL input or output pointer");
+    if (n_local > n) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "n_local > n");
+    if (n > 0xFFFFFFFFull) return set_error(ctx, KTRI_ERR_UNSUPPORTED, "n must be below 2^32 (u32 vertex ids)");
+    if (first_out[0] != 0 || first_out[n] != m)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal m");
+    u64 maxdeg = 0;
+    for (u64 v = 0; v < n; ++v) {
+        if (first_out[v + 1] < first_out[v]) return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out is not monotone");
+        if (v < n_local) maxdeg = std::max<u64>(maxdeg, first_out[v + 1] - first_out[v]);
+    }
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    *kept_count = 0;
+    *edge_count = 0;
+    out_first_out[0] = 0;
+    if (n_local == 0) return KTRI_OK;
+    // lists longer than the block sort's shared memory are sorted through global scratch of
+    // the next power of two, as many at a time as 256 MiB allows
+    u64 P = 1;
+    while (P < maxdeg) P <<= 1;
+    const int big_grid = P <= 8192 ? 1 : (int)std::max<u64>(1, std::min<u64>(ctx->num_sms, (256ull << 20) / (4 * P)));
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes);
+        return at;
+    };
+    const size_t x_ctl = take(sizeof(Control)), x_fo = take(8 * (n + 1)), x_head = take(4 * (m + 1)),
+                 x_cnt = take(8 * (n_local + 1)), x_keep = take(8 * (n_local + 1)),
+                 x_sums = take(8 * (ktri::dag_scan_chunks(n_local) + 1)), x_max = take(8), x_kept = take(4 * n_local),
+                 x_ofo = take(8 * (n_local + 1)), x_ohead = take(4 * (m + 1)), x_desc = take(16 * n_local),
+                 x_mid = take(4 * n_local), x_big = take(4 * n_local),
+                 x_scr = take(P <= 8192 ? 4 : 4 * P * (u64)big_grid);
+    int rc = ensure_ws(ctx, off);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* ctl = reinterpret_cast<Control*>(base + x_ctl);
+    auto* d_fo = reinterpret_cast<u64*>(base + x_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + x_head);
+    auto* d_cnt = reinterpret_cast<u64*>(base + x_cnt);
+    auto* d_keep = reinterpret_cast<u64*>(base + x_keep);
+    auto* d_ofo = reinterpret_cast<u64*>(base + x_ofo);
+    auto* d_ohead = reinterpret_cast<u32*>(base + x_ohead);
+    auto* d_kept = reinterpret_cast<u32*>(base + x_kept);
+    auto* d_max = reinterpret_cast<unsigned long long*>(base + x_max);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
+    KTRI_CK(ctx, cudaMemsetAsync(base + x_desc, 0, 16 * n_local, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, 8 * (n + 1), cudaMemcpyHostToDevice, st));
+    if (m) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, 4 * m, cudaMemcpyHostToDevice, st));
+    ktri::launch_contract(d_fo, d_head, n, n_local, d_cnt, d_keep, reinterpret_cast<u64*>(base + x_sums), d_max,
+                          d_kept, d_ofo, d_ohead, base + x_desc, ctx->num_sms, st);
+    // sorted by id, as preprocessing_global does after compact (cetric.h:916-930)
+    ktri::launch_sort_lists<u64>(n_local, base + x_desc, d_ohead, reinterpret_cast<u32*>(base + x_mid),
+                                 reinterpret_cast<u32*>(base + x_big), reinterpret_cast<u32*>(base + x_scr), P, big_grid,
+                                 ctl, ctx->num_sms, st);
+    KTRI_CK(ctx, cudaGetLastError());
+    u64 ke[2] = {0, 0};
+    KTRI_CK(ctx, cudaMemcpyAsync(&ke[0], d_keep + n_local, 8, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(&ke[1], d_cnt + n_local, 8, cudaMemcpyDeviceToHost, st));
+    u32 err = 0;
+    KTRI_CK(ctx, cudaMemcpyAsync(&err, &ctl->err, 4, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaStreamSynchronize(st));
+    if (err & ktri::DEV_ERR_MASK) return set_error(ctx, KTRI_ERR_CUDA, "list sort found a list above its scratch");
+    const u64 K = ke[0], E = ke[1];
+    if (K) KTRI_CK(ctx, cudaMemcpyAsync(kept_out, d_kept, 4 * K, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(out_first_out, d_ofo, 8 * (K + 1), cudaMemcpyDeviceToHost, st));
+    if (E) KTRI_CK(ctx, cudaMemcpyAsync(out_head, d_ohead, 4 * E, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaStreamSynchronize(st));
+    *kept_count = K;
+    *edge_count = E;
+    return KTRI_OK;
 }
 
 // ---- triangle listing (checking) -----------------------------------------------------------

@@ -129,9 +129,92 @@ __global__ void k_dag_scatter(const u64* __restrict__ fo, const u32* __restrict_
     }
 }
 
+// Contraction, pass 1: per local vertex the number of ghosts in its out-list (the edges that
+// survive), whether it survives, and the longest surviving list.
+__global__ void k_contract_count(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n, u64 n_local,
+                                 u64* __restrict__ cnt, u64* __restrict__ keep, unsigned long long* maxlen) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 v = warp; v < n_local; v += nwarps) {
+        u64 c = 0;
+        for (u64 e = fo[v] + lane; e < fo[v + 1]; e += 32) {
+            const u32 u = head[e];
+            c += (u >= n_local && u < n) ? 1u : 0u;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+        if (lane == 0) {
+            cnt[v] = c;
+            keep[v] = c ? 1ull : 0ull;
+            if (c) atomicMax(maxlen, c);
+        }
+    }
+}
+
+// Contraction, pass 2: the surviving vertices renumbered in order, their ghost lists copied
+// in list order, and one descriptor per surviving list (for the id sort).
+__global__ void k_contract_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n, u64 n_local,
+                                   const u64* __restrict__ cnt_scan, const u64* __restrict__ keep_scan,
+                                   u32* __restrict__ kept, u64* __restrict__ out_fo, u32* __restrict__ out_head,
+                                   Desc<u64>* __restrict__ desc) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    if (warp == 0 && lane == 0) out_fo[keep_scan[n_local]] = cnt_scan[n_local];
+    for (u64 v = warp; v < n_local; v += nwarps) {
+        const u64 base = cnt_scan[v], c = cnt_scan[v + 1] - base;
+        if (c == 0) continue;
+        const u64 k = keep_scan[v];
+        if (lane == 0) {
+            kept[k] = (u32)v;
+            out_fo[k] = base;
+            Desc<u64> d;
+            d.start = base;
+            d.d = (u32)c;
+            d.pad = 0;
+            desc[k] = d;
+        }
+        u64 at = base;
+        for (u64 e0 = fo[v]; e0 < fo[v + 1]; e0 += 32) {
+            const u64 e = e0 + lane;
+            const u32 u = e < fo[v + 1] ? head[e] : 0xFFFFFFFFu;
+            const bool g = u >= n_local && u < n;
+            const u32 ball = __ballot_sync(0xFFFFFFFFu, g);
+            if (g) out_head[at + __popc(ball & ((1u << lane) - 1))] = u;
+            at += __popc(ball);
+        }
+    }
+}
+
 }  // namespace
 
 u64 dag_scan_chunks(u64 n) { return (n + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK; }
+
+void launch_scan_u64(u64* x, u64 len, u64* sums, cudaStream_t st) {
+    if (len == 0) return;
+    const u64 nch = (len + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    k_scan_chunks<<<(unsigned)nch, SCAN_BLOCK, 0, st>>>(x, len, sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, nch);
+    k_scan_add<<<(unsigned)nch, SCAN_BLOCK, 0, st>>>(x, len, sums);
+}
+
+void launch_contract(const u64* fo, const u32* head, u64 n, u64 n_local, u64* cnt, u64* keep, u64* sums,
+                     unsigned long long* maxlen, u32* kept, u64* out_fo, u32* out_head, void* desc, int num_sms,
+                     cudaStream_t st) {
+    if (n_local == 0) return;
+    u64 blocks = (n_local * 32 + 255) / 256;
+    const u64 cap = (u64)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    cudaMemsetAsync(cnt + n_local, 0, sizeof(u64), st);
+    cudaMemsetAsync(keep + n_local, 0, sizeof(u64), st);
+    cudaMemsetAsync(maxlen, 0, sizeof(u64), st);
+    k_contract_count<<<(unsigned)blocks, 256, 0, st>>>(fo, head, n, n_local, cnt, keep, maxlen);
+    launch_scan_u64(cnt, n_local + 1, sums, st);
+    launch_scan_u64(keep, n_local + 1, sums, st);
+    k_contract_scatter<<<(unsigned)blocks, 256, 0, st>>>(fo, head, n, n_local, cnt, keep, kept, out_fo, out_head,
+                                                       reinterpret_cast<Desc<u64>*>(desc));
+}
 
 void launch_dag_symmetrize(const u64* fo, const u32* head, u64 n, u64* fs, u32* hs, u32* cursor, u64* sums,
                            int num_sms, cudaStream_t st) {

@@ -109,6 +109,14 @@ void launch_narrow_ids(const u64* src, u64 count, u32* dst, int num_sms, cudaStr
 // Oriented out-lists -> undirected CSR of their edges (fs: n + 1 offsets, hs: 2m ids).  cursor
 // needs n u32 and sums dag_scan_chunks(n) u64 of scratch.
 u64 dag_scan_chunks(u64 n);
+void launch_scan_u64(u64* x, u64 len, u64* sums, cudaStream_t st);  // exclusive, in place
+// Contraction of a rank's lists after its local phase: local vertices 0..n_local-1 keep their
+// ghost out-neighbours (ids n_local..n-1) in list order; vertices left without any are dropped
+// and the rest renumbered.  cnt and keep need n_local + 1 entries, sums dag_scan_chunks(n_local),
+// desc n_local Desc<u64> (for sorting the lists by id afterwards).
+void launch_contract(const u64* fo, const u32* head, u64 n, u64 n_local, u64* cnt, u64* keep, u64* sums,
+                     unsigned long long* maxlen, u32* kept, u64* out_fo, u32* out_head, void* desc, int num_sms,
+                     cudaStream_t st);
 void launch_dag_symmetrize(const u64* fo, const u32* head, u64 n, u64* fs, u32* hs, u32* cursor, u64* sums,
                            int num_sms, cudaStream_t st);
 void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs, u64 n, u64* totals, Control* ctl,

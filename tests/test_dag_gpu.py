@@ -110,3 +110,59 @@ def test_dag_edge_cases_and_errors(counter):
         assert e.value.code == _native.ERR_INVALID_CSR
     t, _ = counter.count_dag(np.array([0, 2, 3, 3], np.uint64), np.array([2, 1, 2], np.uint32))
     assert t == 1  # the context stays usable after an error
+
+
+def rank_lists(g: Graph, r: int, ranks: int, seed: int):
+    """Rank r's oriented lists with its own vertices numbered first: (fo, head, n_local)."""
+    src, dst = edges_of(g)
+    owner = (np.arange(g.n) * ranks) // g.n
+    keep = (owner[src] == r) | (owner[dst] == r)
+    s, d = src[keep], dst[keep]
+    local = np.flatnonzero(owner == r)
+    ghosts = np.setdiff1d(np.unique(np.concatenate([s, d])), local)
+    order = np.concatenate([local, ghosts])
+    idx = np.full(g.n, -1, dtype=np.int64)
+    idx[order] = np.arange(len(order))
+    deg = np.diff(g.first_out.astype(np.int64))
+    key = deg * (1 << 32) + np.arange(g.n)
+    fo, hd = oriented_lists(len(order), idx[s], idx[d], np.argsort(np.argsort(key[order])), seed=seed)
+    return fo, hd, len(local)
+
+
+@pytest.mark.parametrize("ranks", [2, 4])
+def test_contraction_after_local_phase(counter, ranks):
+    """remove_internal_edges + compact + id sort (cetric.h:872-930): every local vertex keeps
+    its ghost out-neighbours, sorted; vertices left without any are dropped."""
+    g = Graph.rmat(12, 16, seed=21)
+    for r in range(ranks):
+        fo, hd, nl = rank_lists(g, r, ranks, seed=r)
+        kept, cfo, chd = counter.contract_dag(fo, hd, nl)
+        want_kept, want_lists = [], []
+        f = fo.astype(np.int64)
+        for v in range(nl):
+            gl = np.sort(hd[f[v]:f[v + 1]][hd[f[v]:f[v + 1]] >= nl])
+            if len(gl):
+                want_kept.append(v)
+                want_lists.append(gl)
+        assert list(kept) == want_kept
+        assert cfo[0] == 0 and len(cfo) == len(want_kept) + 1
+        assert np.array_equal(np.diff(cfo.astype(np.int64)), [len(x) for x in want_lists])
+        assert np.array_equal(chd, np.concatenate(want_lists) if want_lists else np.zeros(0, np.uint32))
+
+
+def test_contraction_edge_cases(counter):
+    kept, cfo, chd = counter.contract_dag(np.array([0, 1, 1], np.uint64), np.array([1], np.uint32), 2)
+    assert len(kept) == 0 and list(cfo) == [0] and len(chd) == 0       # no ghosts: nothing survives
+    kept, cfo, chd = counter.contract_dag(np.array([0, 0, 0], np.uint64), np.zeros(0, np.uint32), 0)
+    assert len(kept) == 0 and list(cfo) == [0]
+    # a hub with a long ghost list (sorted through global scratch) next to short ones
+    nl, ng = 3, 20000
+    rng = np.random.default_rng(2)
+    lists = [rng.permutation(np.arange(nl, nl + ng)).astype(np.uint32), np.array([nl + 5, 1], np.uint32),
+             np.zeros(0, np.uint32)]
+    fo = np.zeros(nl + ng + 1, np.uint64)
+    fo[1:nl + 1] = np.cumsum([len(x) for x in lists])
+    fo[nl + 1:] = fo[nl]
+    kept, cfo, chd = counter.contract_dag(fo, np.concatenate(lists), nl)
+    assert list(kept) == [0, 1] and list(cfo) == [0, ng, ng + 1]
+    assert np.array_equal(chd[:ng], np.arange(nl, nl + ng)) and chd[ng] == nl + 5
