@@ -220,6 +220,25 @@ int ktri_contract_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32
                           uint64_t m, uint32_t* kept_out, uint64_t* out_first_out, uint32_t* out_head,
                           uint64_t* kept_count, uint64_t* edge_count);
 
+/* ---- load-balancing cost functions -------------------------------------------------------
+ * The reference balances work across ranks by a per-vertex cost (cost_function.h:287-376,
+ * chosen with --cost-function): N (1), D (degree), DH (out-degree), DDH (degree x out-degree),
+ * DH2 (out-degree^2), DPD (sum over higher neighbours u of d+(v) + d+(u), the edge iterator's
+ * merge work), IDPD (the same over lower neighbours).  Orientation is (degree, id).
+ * ktri_partition_cost computes the costs on the device and cuts the vertex range into `parts`
+ * ranges of about equal total cost: boundaries_out[0] = 0 <= ... <= boundaries_out[parts] = n.
+ * costs_out (n entries) is optional. */
+#define KTRI_COST_N 0
+#define KTRI_COST_D 1
+#define KTRI_COST_DH 2
+#define KTRI_COST_DDH 3
+#define KTRI_COST_DH2 4
+#define KTRI_COST_DPD 5
+#define KTRI_COST_IDPD 6
+int ktri_partition_cost(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                        int32_t cost_function, uint32_t parts, uint64_t* boundaries_out, uint64_t* costs_out,
+                        uint64_t* total_cost_out);
+
 /* ---- autotuning ---------------------------------------------------------------------------
  * No counterpart in the reference (its strategy is a command-line choice, --intersection-method,
  * apps/parse_parameters.h:156-158).  ktri_autotune times candidate configurations of one count

@@ -137,6 +137,7 @@ SIGNATURES = {
     "ktri_count_dag_device": (ctypes.c_int, [P, P, P, U64, U64, P, P, ctypes.POINTER(Opts), P]),
     "ktri_contract_dag_ctx": (ctypes.c_int, [P, P, P, U64, U64, U64, P, P, P, ctypes.POINTER(U64),
                                              ctypes.POINTER(U64)]),
+    "ktri_partition_cost": (ctypes.c_int, [P, P, P, U64, U64, I32, U32, P, P, ctypes.POINTER(U64)]),
     "ktri_autotune": (ctypes.c_int, [P, P, P, U64, U64, P, U64, CP, ctypes.POINTER(Opts), ctypes.POINTER(Tuning), P]),
     "ktri_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ServerOpts), PP]),
     "ktri_server_submit": (ctypes.c_int, [P, U64, P, P, U64, U64, U32, ctypes.POINTER(U64)]),

@@ -222,6 +222,23 @@ class TriangleCounter:
                                                   ctypes.byref(k), ctypes.byref(e)))
         return kept[: k.value].copy(), ofo[: k.value + 1].copy(), oh[: e.value].copy()
 
+    COST_FUNCTIONS = {"N": 0, "D": 1, "DH": 2, "DDH": 3, "DH2": 4, "DPD": 5, "IDPD": 6}
+
+    def partition_cost(self, first_out, head, cost_function: str = "DPD", parts: int = 1, costs: bool = False):
+        """The reference's load-balancing cost functions (cost_function.h:287-376) on the device:
+        (boundaries of `parts` vertex ranges of about equal cost, total cost, per-vertex costs
+        or None)."""
+        fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        hd = np.ascontiguousarray(head, dtype=np.uint32)
+        n, nnz = len(fo) - 1, len(hd)
+        bnd = np.zeros(parts + 1, dtype=np.uint64)
+        cst = np.zeros(max(1, n), dtype=np.uint64) if costs else None
+        total = ctypes.c_uint64(0)
+        self._check(self._L.ktri_partition_cost(self._ctx, fo.ctypes.data, hd.ctypes.data if nnz else None, n, nnz,
+                                                self.COST_FUNCTIONS[cost_function], parts, bnd.ctypes.data,
+                                                cst.ctypes.data if cst is not None else None, ctypes.byref(total)))
+        return bnd, int(total.value), (cst[:n] if cst is not None else None)
+
     def count_dag_device(self, first_out_ptr: int, head_ptr: int, n: int, m: int, total_ptr: int,
                          per_vertex_ptr: int | None = None, conf: Config | None = None, stream: int = 0) -> None:
         conf = conf or Config()

@@ -209,8 +209,8 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
                             opt.medium_outdegree, opt.segment, ctl, sms, st);
     if (autom)
-        ktri::launch_order_tiles(fo, head, n, ltiles, opt.segment, reinterpret_cast<u32*>(base + L.thist), lsorted,
-                                 ctl, sms, st);
+        ktri::launch_order_tiles(fo, head, n, ltiles, &ctl->large_tiles, opt.segment,
+                                 reinterpret_cast<u32*>(base + L.thist), lsorted, ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -776,6 +776,62 @@ int ktri_contract_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32
     KTRI_CK(ctx, cudaStreamSynchronize(st));
     *kept_count = K;
     *edge_count = E;
+    return KTRI_OK;
+}
+
+// ---- load-balancing cost functions -------------------------------------------------------------
+
+int ktri_partition_cost(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
+                        int32_t cost_function, uint32_t parts, uint64_t* boundaries_out, uint64_t* costs_out,
+                        uint64_t* total_cost_out) {
+    ktri::Options opt;
+    opt.method = KTRI_METHOD_MERGE;
+    int rc = check_common(ctx, first_out, head, n, nnz, total_cost_out, opt);
+    if (rc) return rc;
+    if (!boundaries_out || parts == 0) return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "need parts >= 1 boundaries");
+    if (cost_function < KTRI_COST_N || cost_function > KTRI_COST_IDPD)
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "unknown cost function");
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    *total_cost_out = 0;
+    if (n == 0) {
+        for (u32 i = 0; i <= parts; ++i) boundaries_out[i] = 0;
+        return KTRI_OK;
+    }
+    if (first_out[0] != 0 || first_out[n] != nnz)
+        return set_error(ctx, KTRI_ERR_INVALID_CSR, "first_out[0] must be 0 and first_out[n] must equal nnz");
+    Layout L = make_layout(n, nnz, KTRI_METHOD_MERGE, ctx->num_sms, true, true);
+    const size_t x_cost = L.bytes, x_sums = align_up(x_cost + 8 * (n + 1)),
+                 x_bnd = align_up(x_sums + 8 * (ktri::dag_scan_chunks(n) + 1));
+    L.bytes = align_up(x_bnd + 8 * ((u64)parts + 1));
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->ws);
+    auto* d_fo = reinterpret_cast<u64*>(base + L.in_fo);
+    auto* d_head = reinterpret_cast<u32*>(base + L.in_head);
+    auto* d_cost = reinterpret_cast<u64*>(base + x_cost);
+    cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, 8 * (n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, 4 * nnz, cudaMemcpyHostToDevice, st));
+    // degrees and out-degrees come from the orientation stage of the pipeline
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, reinterpret_cast<u64*>(base + L.total),
+                                    reinterpret_cast<u64*>(base + L.cnt), opt, st, true)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, reinterpret_cast<u64*>(base + L.total),
+                                    reinterpret_cast<u64*>(base + L.cnt), opt, st, true);
+    if (rc) return rc;
+    ktri::launch_cost_partition(d_fo, d_head, n, reinterpret_cast<const u32*>(base + L.deg),
+                                reinterpret_cast<const u32*>(base + L.dplus), cost_function, parts, d_cost,
+                                reinterpret_cast<u64*>(base + x_sums), reinterpret_cast<u64*>(base + x_bnd),
+                                ctx->num_sms, st);
+    KTRI_CK(ctx, cudaGetLastError());
+    std::vector<u64> prefix(costs_out ? n + 1 : 0);
+    if (costs_out) KTRI_CK(ctx, cudaMemcpyAsync(prefix.data(), d_cost, 8 * (n + 1), cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(total_cost_out, d_cost + n, 8, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaMemcpyAsync(boundaries_out, base + x_bnd, 8 * ((u64)parts + 1), cudaMemcpyDeviceToHost, st));
+    rc = device_status(ctx);
+    if (rc) return rc;
+    if (costs_out)
+        for (u64 v = 0; v < n; ++v) costs_out[v] = prefix[v + 1] - prefix[v];
     return KTRI_OK;
 }
 

@@ -10,6 +10,7 @@
 // Vertex v's undirected list is its out-list (in the given order) followed by its in-list
 // (in arrival order).  Entries that are out of range or self-loops are copied into the out
 // part as they are, so the pipeline's validation reports them; they get no in-list entry.
+#include "ktri.h"
 #include "ktri_device.cuh"
 #include "ktri_kernels.h"
 
@@ -187,9 +188,68 @@ __global__ void k_contract_scatter(const u64* __restrict__ fo, const u32* __rest
     }
 }
 
+// Per-vertex cost of the reference's load-balancing cost functions (cost_function.h:287-345),
+// one warp per vertex; deg = undirected degree, dplus = out-degree in (degree, id) order.
+__global__ void k_vertex_cost(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
+                              const u32* __restrict__ deg, const u32* __restrict__ dplus, int fn, u64* __restrict__ cost) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 v = warp; v < n; v += nwarps) {
+        const u64 dv = deg[v], ov = dplus[v];
+        u64 c = 0;
+        if (fn == KTRI_COST_DPD || fn == KTRI_COST_IDPD) {
+            const bool higher = fn == KTRI_COST_DPD;
+            for (u64 e = fo[v] + lane; e < fo[v + 1]; e += 32) {
+                const u32 u = head[e];
+                if (u >= n) continue;
+                const bool above = key_less(dv, v, deg[u], u);  // (deg u, u) > (deg v, v)
+                if (above == higher) c += ov + dplus[u];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+        } else {
+            c = fn == KTRI_COST_N ? 1 : fn == KTRI_COST_D ? dv : fn == KTRI_COST_DH ? ov : fn == KTRI_COST_DDH ? dv * ov : ov * ov;
+        }
+        if (lane == 0) cost[v] = c;
+    }
+}
+
+// boundaries[i] = first vertex whose cost prefix reaches i / parts of the total (prefix holds
+// the exclusive prefix sums, prefix[n] = total); boundaries[parts] = n.
+__global__ void k_cost_boundaries(const u64* __restrict__ prefix, u64 n, u32 parts, u64* __restrict__ boundaries) {
+    const u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > parts) return;
+    if (i == parts) {
+        boundaries[i] = n;
+        return;
+    }
+    const u64 total = prefix[n];
+    const u64 target = (u64)(((unsigned __int128)total * i + parts - 1) / parts);
+    u64 lo = 0, hi = n;  // smallest v with prefix[v] >= target
+    while (lo < hi) {
+        const u64 mid = (lo + hi) >> 1;
+        if (prefix[mid] >= target) hi = mid;
+        else lo = mid + 1;
+    }
+    boundaries[i] = lo;
+}
+
 }  // namespace
 
 u64 dag_scan_chunks(u64 n) { return (n + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK; }
+
+void launch_cost_partition(const u64* fo, const u32* head, u64 n, const u32* deg, const u32* dplus, int fn, u32 parts,
+                           u64* cost, u64* sums, u64* boundaries, int num_sms, cudaStream_t st) {
+    if (n == 0) return;
+    u64 blocks = (n * 32 + 255) / 256;
+    const u64 cap = (u64)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    cudaMemsetAsync(cost + n, 0, sizeof(u64), st);
+    k_vertex_cost<<<(unsigned)blocks, 256, 0, st>>>(fo, head, n, deg, dplus, fn, cost);
+    launch_scan_u64(cost, n + 1, sums, st);
+    k_cost_boundaries<<<(unsigned)((parts + 1 + 255) / 256), 256, 0, st>>>(cost, n, parts, boundaries);
+}
 
 void launch_scan_u64(u64* x, u64 len, u64* sums, cudaStream_t st) {
     if (len == 0) return;

@@ -81,11 +81,11 @@ template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
                  u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st);
 
-// Large-owner tiles reordered by the first vertex their segment streams (hist needs
-// tile_order_scratch_words() u32, sorted the same capacity as tiles).
+// Owner tiles reordered by the first vertex their segment streams (*count tiles on the device;
+// hist needs tile_order_scratch_words() u32, sorted the same capacity as tiles).
 u64 tile_order_scratch_words();
-void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, u32 seg, u32* hist,
-                        uint2* sorted, Control* ctl, int num_sms, cudaStream_t st);
+void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, const unsigned long long* count,
+                        u32 seg, u32* hist, uint2* sorted, Control* ctl, int num_sms, cudaStream_t st);
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
@@ -110,6 +110,10 @@ void launch_narrow_ids(const u64* src, u64 count, u32* dst, int num_sms, cudaStr
 // needs n u32 and sums dag_scan_chunks(n) u64 of scratch.
 u64 dag_scan_chunks(u64 n);
 void launch_scan_u64(u64* x, u64 len, u64* sums, cudaStream_t st);  // exclusive, in place
+// Per-vertex cost (KTRI_COST_*) into cost[0..n), its exclusive prefix in place (cost[n] = total),
+// and parts + 1 vertex boundaries of equal-cost ranges.  sums: dag_scan_chunks(n) u64.
+void launch_cost_partition(const u64* fo, const u32* head, u64 n, const u32* deg, const u32* dplus, int fn, u32 parts,
+                           u64* cost, u64* sums, u64* boundaries, int num_sms, cudaStream_t st);
 // Contraction of a rank's lists after its local phase: local vertices 0..n_local-1 keep their
 // ghost out-neighbours (ids n_local..n-1) in list order; vertices left without any are dropped
 // and the rest renumbered.  cnt and keep need n_local + 1 entries, sums dag_scan_chunks(n_local),

@@ -255,9 +255,10 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
 constexpr u32 TILE_BUCKETS = 4096;
 
 __global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head,
-                            const uint2* __restrict__ tiles, u32 seg, u32 shift, u32* hist, Control* ctl) {
+                            const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
+                            u32* hist, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
-    const u64 nt = *(volatile unsigned long long*)&ctl->large_tiles;
+    const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
         const uint2 tl = tiles[t];
@@ -287,9 +288,10 @@ __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
 }
 
 __global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const uint2* __restrict__ tiles,
-                               u32 seg, u32 shift, u32* cursor, uint2* __restrict__ sorted, Control* ctl) {
+                               const unsigned long long* count, u32 seg, u32 shift, u32* cursor,
+                               uint2* __restrict__ sorted, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
-    const u64 nt = *(volatile unsigned long long*)&ctl->large_tiles;
+    const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
         const uint2 tl = tiles[t];
@@ -303,16 +305,16 @@ __global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict
 
 u64 tile_order_scratch_words() { return TILE_BUCKETS; }
 
-void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, u32 seg, u32* hist,
-                        uint2* sorted, Control* ctl, int num_sms, cudaStream_t st) {
+void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, const unsigned long long* count,
+                        u32 seg, u32* hist, uint2* sorted, Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u32 bits = 0;
     while ((1ull << bits) < n) ++bits;
     const u32 shift = bits > 12 ? bits - 12 : 0;
     cudaMemsetAsync(hist, 0, sizeof(u32) * TILE_BUCKETS, st);
-    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, seg, shift, hist, ctl);
+    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, count, seg, shift, hist, ctl);
     k_tile_scan<<<1, 1024, 0, st>>>(hist, ctl);
-    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, seg, shift, hist, sorted, ctl);
+    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, count, seg, shift, hist, sorted, ctl);
 }
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,

@@ -287,3 +287,32 @@ def test_count_binary_file_errors(counter, tmp_path):
     with pytest.raises(KtriError) as e:
         counter.count_binary_file(stem)
     assert e.value.code == _native.ERR_INVALID_CSR
+
+
+@pytest.mark.parametrize("fn", ["N", "D", "DH", "DDH", "DH2", "DPD", "IDPD"])
+def test_cost_functions_and_partition(counter, fn):
+    """The reference's load-balancing costs (cost_function.h:287-376), computed on the device,
+    against numpy; the cut points split the cost prefix evenly."""
+    g = Graph.rmat(12, 16, seed=8)
+    fo = g.first_out.astype(np.int64)
+    n = g.n
+    deg = np.diff(fo)
+    src = np.repeat(np.arange(n), deg)
+    dst = g.head.astype(np.int64)
+    key = deg * (1 << 32) + np.arange(n)
+    up = key[dst] > key[src]
+    dplus = np.bincount(src[up], minlength=n)
+    if fn in ("DPD", "IDPD"):
+        sel = up if fn == "DPD" else ~up
+        want = np.bincount(src[sel], weights=(dplus[src] + dplus[dst])[sel], minlength=n).astype(np.int64)
+    else:
+        want = {"N": np.ones(n, np.int64), "D": deg, "DH": dplus, "DDH": deg * dplus, "DH2": dplus * dplus}[fn]
+    parts = 7
+    bnd, total, cost = counter.partition_cost(g.first_out, g.head, fn, parts, costs=True)
+    assert np.array_equal(cost.astype(np.int64), want) and total == int(want.sum())
+    prefix = np.concatenate([[0], np.cumsum(want)])
+    assert bnd[0] == 0 and bnd[-1] == n and np.all(np.diff(bnd.astype(np.int64)) >= 0)
+    for i in range(1, parts):
+        b = int(bnd[i])
+        target = -(-total * i // parts)
+        assert prefix[b] >= target and (b == 0 or prefix[b - 1] < target)
