@@ -145,6 +145,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over all ranks (a replicated job takes as long as its slowest rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(m: int, ms: float, ws: int) -> float:
+    """Whole-job edges/s of ws replicas that each count an m-edge graph in ms (the max over ranks)."""
+    return ws * m / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -417,11 +433,11 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args)
         return
-    if WORKLOADS[args.workload]["kind"] == "batch":
-        run_batch(args)
-        return
-    if WORKLOADS[args.workload]["kind"] == "serve":
-        run_serve(args)
+    if WORKLOADS[args.workload]["kind"] in ("batch", "serve"):
+        # the batched and served forms measure one GPU; under torchrun rank 0 runs them
+        if dist_env()[1] != 0:
+            return
+        (run_batch if WORKLOADS[args.workload]["kind"] == "batch" else run_serve)(args)
         return
 
     import torch
@@ -492,13 +508,8 @@ def main():
     ctr.check()
     assert int(tot_d.item()) == total_ref and torch.equal(pv_d, pv_ref), "result changed between steps"
 
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-
-    value = ws * g.m / (ms / 1e3)
+    ms = max_over_ranks(ms, f"cuda:{dev}")
+    value = replica_value(g.m, ms, ws)
 
     # e2e through the public host-buffer API, pinned host memory, copies inside the region
     fo_h = torch.from_numpy(g.first_out.view(np.int64)).pin_memory()
@@ -525,12 +536,8 @@ def main():
     barrier()
     e2e_ms = (t1 - t0) * 1e3 / e2e_steps
     assert tot.value == total_ref
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = ws * g.m / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(e2e_ms, f"cuda:{dev}")
+    e2e_value = replica_value(g.m, e2e_ms, ws)
 
     if rank != 0:
         if ws > 1:
