@@ -383,10 +383,10 @@ def run_serve(args):
         th.join()
         return time.perf_counter() - start, lat
 
-    with Server(memory_budget=w["budget"]) as srv:
+    with Server(memory_budget=w["budget"], direct_host_access=args.serve_direct) as srv:
         wall, lat = replay(srv, paced=True)
         st = srv.stats()
-    with Server(memory_budget=w["budget"]) as srv:
+    with Server(memory_budget=w["budget"], direct_host_access=args.serve_direct) as srv:
         sat_wall, _ = replay(srv, paced=False)
         sat_st = srv.stats()
     ctr = TriangleCounter(0)
@@ -404,6 +404,7 @@ def run_serve(args):
         "ms_per_step": wall * 1e3 / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded generators)",
         "config": {"workload": "serve", "rate_per_s": w["rate"], "seconds": seconds, "requests": k,
+                   "host_copies": "device reads host memory where it can" if args.serve_direct else "pinned staging",
                    "distinct_graphs": len(specs), "m_total": m_total, "median_m": w["median_m"], "sigma": w["sigma"],
                    "repeat": w["repeat"], "memory_budget": w["budget"], "generation_s": round(gen_s, 1)},
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
@@ -427,6 +428,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--serve-seconds", type=float, default=0.0, help="duration of the served stream (default 60)")
+    ap.add_argument("--serve-direct", action="store_true",
+                    help="let the GPU read and write the requests' host memory directly where it can")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

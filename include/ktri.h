@@ -283,7 +283,12 @@ typedef struct ktri_server_opts {
     uint64_t memory_budget;      /* device bytes for resident graphs and batches (default 120 GiB) */
     uint64_t max_batch_nnz;      /* adjacency entries per batch (default 2^28) */
     uint32_t max_batch_graphs;   /* graphs per batch (default 4096) */
-    uint32_t reserved[7];
+    uint32_t direct_host_access; /* 1: where the device reads pageable host memory (Grace + Blackwell), kernels
+                                    gather the callers' graphs and write per-vertex counts straight into host
+                                    memory; 0 (default): batches go through pinned host staging.  Direct access
+                                    lowers latency at low load, but the driver may migrate the touched pages to
+                                    the GPU, which slows the callers' later host accesses */
+    uint32_t reserved[6];
 } ktri_server_opts;
 typedef struct ktri_server_stats {
     uint64_t submitted, completed, batches, batched_graphs, cache_hits, evictions, resident_graphs, resident_bytes,

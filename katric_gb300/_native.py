@@ -61,7 +61,8 @@ class ServerOpts(ctypes.Structure):
         ("memory_budget", ctypes.c_uint64),
         ("max_batch_nnz", ctypes.c_uint64),
         ("max_batch_graphs", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 7),
+        ("direct_host_access", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 6),
     ]
 
 

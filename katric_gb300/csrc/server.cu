@@ -44,6 +44,80 @@ __global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64
     }
 }
 
+// Where the device reads pageable host memory (ATS/HMM over NVLink-C2C on Grace + Blackwell),
+// a batch is gathered straight from the callers' arrays: no host-side packing pass.
+struct GraphSrc {
+    const u64* fo;  // the caller's first_out (n + 1 entries), host memory
+    const u32* head;
+    u64* pv_out;    // where the per-vertex counts go (host memory), or null
+};
+
+// The warp's 256 consecutive union elements at base: lane handles base + lane + 32 j, so each
+// load instruction of the warp reads 128 consecutive bytes.  first[g] is the union offset of
+// graph g (first[k] = total); g starts at the warp's first element's graph.
+__device__ __forceinline__ u64 warp_graph_of(const u64* first, u64 k, u64 x) {
+    u64 lo = 0, hi = k;  // first[lo] <= x < first[hi]
+    while (hi - lo > 1) {
+        const u64 mid = (lo + hi) >> 1;
+        if (first[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_gather(const GraphSrc* __restrict__ src, const u64* __restrict__ vf, const u64* __restrict__ ef,
+                         u64 k, u64 n, u64 nnz, u64* __restrict__ dfo, u32* __restrict__ dhead) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    if (warp == 0 && lane == 0) dfo[0] = 0;
+    for (u64 base = warp * 256; base < nnz; base += nwarps * 256) {
+        u64 g = 0;
+        if (lane == 0) g = warp_graph_of(ef, k, base);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+#pragma unroll 4
+        for (int j = 0; j < 8; ++j) {
+            const u64 e = base + lane + 32 * j;
+            if (e >= nnz) break;
+            while (e >= ef[g + 1]) ++g;
+            dhead[e] = src[g].head[e - ef[g]] + (u32)vf[g];
+        }
+    }
+    for (u64 base = warp * 256; base < n; base += nwarps * 256) {
+        u64 g = 0;
+        if (lane == 0) g = warp_graph_of(vf, k, base);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+#pragma unroll 4
+        for (int j = 0; j < 8; ++j) {
+            const u64 v = base + lane + 32 * j;
+            if (v >= n) break;
+            while (v >= vf[g + 1]) ++g;
+            dfo[v + 1] = src[g].fo[v - vf[g] + 1] + ef[g];
+        }
+    }
+}
+
+// Per-vertex counts of the union written into each wanting request's host buffer.
+__global__ void k_scatter_pv(const GraphSrc* __restrict__ src, const u64* __restrict__ vf, u64 k, u64 n,
+                             const u64* __restrict__ pv) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 base = warp * 256; base < n; base += nwarps * 256) {
+        u64 g = 0;
+        if (lane == 0) g = warp_graph_of(vf, k, base);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+#pragma unroll 4
+        for (int j = 0; j < 8; ++j) {
+            const u64 v = base + lane + 32 * j;
+            if (v >= n) break;
+            while (v >= vf[g + 1]) ++g;
+            u64* out = src[g].pv_out;
+            if (out) out[v - vf[g]] = pv[v];
+        }
+    }
+}
+
 // The caller's own CSR of one graph of a rebased union (the inverse of k_rebase for it).
 __global__ void k_unbase(u64* __restrict__ dfo, u32* __restrict__ dhead, const u64* __restrict__ sfo,
                          const u32* __restrict__ shead, u64 n, u64 nnz, u64 vb, u64 eb) {
@@ -72,6 +146,8 @@ struct Request {
     std::vector<uint64_t> pv;
     std::vector<Request*> followers;  // later requests for the same key, answered with this one
     bool follower_pv = false;         // a follower wants the per-vertex counts
+    bool pv_written = false;          // the batch wrote the per-vertex counts into pv directly
+    bool pv_wanted = false;           // want_pv or follower_pv when the batch was formed (under the lock)
 };
 
 struct Resident {  // a graph kept on the device with its counts
@@ -95,8 +171,9 @@ struct Slot {
     void* host = nullptr;
     size_t host_bytes = 0;
     u64 n_total = 0, nnz_total = 0;
-    size_t off_fo = 0, off_head = 0, off_vf = 0, off_ef = 0, off_tot = 0, off_pv = 0;
+    size_t off_fo = 0, off_head = 0, off_vf = 0, off_ef = 0, off_tot = 0, off_pv = 0, off_src = 0;
     size_t h_tot = 0, h_pv = 0;
+    bool direct = false;  // this batch was gathered from host memory by the device
 };
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
@@ -105,6 +182,7 @@ size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct ktri_server {
     int device = 0;
+    bool pageable = false;  // the device reads pageable host memory
     ktri_server_opts opts{};
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -264,27 +342,27 @@ int launch_batch(ktri_server* s, Slot& sl) {
     sl.off_ef = take(8 * (k + 1));
     sl.off_tot = take(8 * k);
     sl.off_pv = take(8 * (n + 1));
+    sl.off_src = take(sizeof(GraphSrc) * (k + 1));
     int rc = grow(&sl.dev, &sl.dev_bytes, off, false);
     if (rc) return rc;
-    // host staging: [fo][head][vf][ef] then read-back [tot][pv]
+    sl.direct = s->pageable && s->opts.direct_host_access;
+    // host staging: [fo][head] (staged batches only), [vf][ef][sources], then read-back [tot][pv]
     size_t hoff = 0;
     auto htake = [&](size_t b) {
         size_t at = hoff;
         hoff = al(hoff + b);
         return at;
     };
-    const size_t h_fo = htake(8 * (n + 1)), h_head = htake(4 * (nnz + 1)), h_vf = htake(8 * (k + 1)),
-                 h_ef = htake(8 * (k + 1));
+    const size_t h_fo = sl.direct ? 0 : htake(8 * (n + 1)), h_head = sl.direct ? 0 : htake(4 * (nnz + 1));
+    const size_t h_vf = htake(8 * (k + 1)), h_ef = htake(8 * (k + 1)), h_src = htake(sizeof(GraphSrc) * (k + 1));
     sl.h_tot = htake(8 * k);
-    sl.h_pv = htake(8 * (n + 1));
+    sl.h_pv = sl.direct ? 0 : htake(8 * (n + 1));
     rc = grow(&sl.host, &sl.host_bytes, hoff, true);
     if (rc) return rc;
     char* h = static_cast<char*>(sl.host);
-    u64* hfo = reinterpret_cast<u64*>(h + h_fo);
-    u32* hhead = reinterpret_cast<u32*>(h + h_head);
     u64* hvf = reinterpret_cast<u64*>(h + h_vf);
     u64* hef = reinterpret_cast<u64*>(h + h_ef);
-    hfo[0] = 0;
+    auto* hsrc = reinterpret_cast<GraphSrc*>(h + h_src);
     u64 vb = 0, eb = 0;
     for (u64 i = 0; i < k; ++i) {
         Request* r = sl.reqs[i];
@@ -292,29 +370,66 @@ int launch_batch(ktri_server* s, Slot& sl) {
         hef[i] = eb;
         vb += r->n;
         eb += r->nnz;
+        r->pv_written = false;
+        if (sl.direct) {
+            if (r->pv_wanted && r->n) {
+                r->pv.resize(r->n);
+                r->pv_written = true;
+            }
+            hsrc[i].fo = reinterpret_cast<const u64*>(r->bfo);
+            hsrc[i].head = r->bhead;
+            hsrc[i].pv_out = r->pv_written ? reinterpret_cast<u64*>(r->pv.data()) : nullptr;
+        }
     }
     hvf[k] = vb;
     hef[k] = eb;
-    // pack the graphs into pinned staging in parallel (ids are rebased on the device)
-#pragma omp parallel for schedule(dynamic, 1) if (k > 1 && nnz > (1u << 16))
-    for (int64_t ii = 0; ii < (int64_t)k; ++ii) {
-        const Request* r = sl.reqs[(size_t)ii];
-        std::memcpy(hfo + hvf[ii] + 1, r->bfo + 1, 8 * r->n);
-        if (r->nnz) std::memcpy(hhead + hef[ii], r->bhead, 4 * r->nnz);
-    }
     char* d = static_cast<char*>(sl.dev);
     cudaStream_t st = sl.stream;
     cudaStreamWaitEvent(st, sl.cache_done, 0);  // earlier resident copies read these buffers
-    cudaMemcpyAsync(d + sl.off_fo, hfo, 8 * (n + 1), cudaMemcpyHostToDevice, st);
-    if (nnz) cudaMemcpyAsync(d + sl.off_head, hhead, 4 * nnz, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d + sl.off_vf, hvf, 8 * (k + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d + sl.off_ef, hef, 8 * (k + 1), cudaMemcpyHostToDevice, st);
     auto* dfo = reinterpret_cast<u64*>(d + sl.off_fo);
     auto* dhead = reinterpret_cast<u32*>(d + sl.off_head);
     auto* dvf = reinterpret_cast<u64*>(d + sl.off_vf);
     auto* def = reinterpret_cast<u64*>(d + sl.off_ef);
-    const unsigned blocks = (unsigned)std::min<u64>(k, 4096);
-    k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k);
+    auto* dsrc = reinterpret_cast<GraphSrc*>(d + sl.off_src);
+    cudaMemcpyAsync(dvf, hvf, 8 * (k + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(def, hef, 8 * (k + 1), cudaMemcpyHostToDevice, st);
+    if (sl.direct) {
+        cudaMemcpyAsync(dsrc, hsrc, sizeof(GraphSrc) * k, cudaMemcpyHostToDevice, st);
+        const u64 warps = (std::max<u64>(n, nnz) + 255) / 256;
+        const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
+        k_gather<<<blocks, 256, 0, st>>>(dsrc, dvf, def, k, n, nnz, dfo, dhead);
+    } else {
+        u64* hfo = reinterpret_cast<u64*>(h + h_fo);
+        u32* hhead = reinterpret_cast<u32*>(h + h_head);
+        hfo[0] = 0;
+        // pack the graphs into pinned staging in parallel, in pieces of at most 4 MiB so that a
+        // large graph is copied by many threads (one host thread copies only ~13 GB/s); ids
+        // are rebased on the device
+        struct Piece {
+            char* dst;
+            const char* src;
+            size_t bytes;
+        };
+        std::vector<Piece> pieces;
+        constexpr size_t PIECE = 4u << 20;
+        auto add = [&](void* dst, const void* src, size_t bytes) {
+            for (size_t o = 0; o < bytes; o += PIECE)
+                pieces.push_back({static_cast<char*>(dst) + o, static_cast<const char*>(src) + o,
+                                  std::min(PIECE, bytes - o)});
+        };
+        for (u64 i = 0; i < k; ++i) {
+            const Request* r = sl.reqs[i];
+            add(hfo + hvf[i] + 1, r->bfo + 1, 8 * r->n);
+            if (r->nnz) add(hhead + hef[i], r->bhead, 4 * r->nnz);
+        }
+#pragma omp parallel for schedule(dynamic, 1) if (pieces.size() > 1 && nnz > (1u << 16))
+        for (int64_t p = 0; p < (int64_t)pieces.size(); ++p)
+            std::memcpy(pieces[(size_t)p].dst, pieces[(size_t)p].src, pieces[(size_t)p].bytes);
+        cudaMemcpyAsync(dfo, hfo, 8 * (n + 1), cudaMemcpyHostToDevice, st);
+        if (nnz) cudaMemcpyAsync(dhead, hhead, 4 * nnz, cudaMemcpyHostToDevice, st);
+        const unsigned blocks = (unsigned)std::min<u64>(k, 4096);
+        k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k);
+    }
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
     ktri_opts o{};
     o.struct_size = sizeof(ktri_opts);
@@ -324,7 +439,13 @@ int launch_batch(ktri_server* s, Slot& sl) {
                                  reinterpret_cast<uint64_t*>(d + sl.off_pv), &o, st);
     if (rc) return rc;
     cudaMemcpyAsync(h + sl.h_tot, d + sl.off_tot, 8 * k, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
+    if (sl.direct) {
+        const u64 warps = (n + 255) / 256;
+        const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
+        k_scatter_pv<<<blocks, 256, 0, st>>>(dsrc, dvf, k, n, reinterpret_cast<const u64*>(d + sl.off_pv));
+    } else {
+        cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
+    }
     cudaEventRecord(sl.done, st);
     return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
 }
@@ -342,7 +463,16 @@ void harvest(ktri_server* s, Slot& sl) {
         Request* r = sl.reqs[i];
         if (rc == KTRI_OK) {
             r->total = tot[i];
-            if (r->want_pv || r->follower_pv) r->pv.assign(pv + vb, pv + vb + r->n);
+            if (sl.direct) {
+                // a follower that asked for counts after the batch started: read them back now
+                if ((r->want_pv || r->follower_pv) && !r->pv_written && r->n) {
+                    r->pv.resize(r->n);
+                    cudaMemcpy(r->pv.data(), static_cast<const char*>(sl.dev) + sl.off_pv + 8 * vb, 8 * r->n,
+                               cudaMemcpyDeviceToHost);
+                }
+            } else if (r->want_pv || r->follower_pv) {
+                r->pv.assign(pv + vb, pv + vb + r->n);
+            }
             keep_resident(s, r, sl, vb, eb, inflight);
         }
         vb += r->n;
@@ -420,6 +550,7 @@ void worker_main(ktri_server* s) {
                 for (Request* r : batch) finish(s, r, KTRI_ERR_OUT_OF_MEMORY);
                 s->cv_done.notify_all();
             } else {
+                for (Request* r : batch) r->pv_wanted = r->want_pv || r->follower_pv;
                 free_slot->reqs = batch;
                 free_slot->busy = true;
                 s->st.batches++;
@@ -470,8 +601,15 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
         if (opts->memory_budget) s->opts.memory_budget = opts->memory_budget;
         if (opts->max_batch_nnz) s->opts.max_batch_nnz = opts->max_batch_nnz;
         if (opts->max_batch_graphs) s->opts.max_batch_graphs = opts->max_batch_graphs;
+        s->opts.direct_host_access = opts->direct_host_access;
     }
     if (s->opts.slots > 8) s->opts.slots = 8;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    s->pageable = pageable == 1;
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(device);

@@ -15,12 +15,14 @@ def graph_mix(count, seed):
     return [b.graph(i) for i in range(b.num_graphs)]
 
 
-def test_results_alone_equal_results_in_the_mix():
+@pytest.mark.parametrize("direct", [False, True])
+def test_results_alone_equal_results_in_the_mix(direct):
     graphs = graph_mix(90, seed=31) + [Graph.rmat(15, 16, seed=3), Graph(np.zeros(5, np.uint64),
                                                                           np.zeros(0, np.uint32))]
     with TriangleCounter(0) as ctr:
         alone = [ctr.count(g.first_out, g.head) for g in graphs]
-    with Server(slots=2, max_batch_nnz=1 << 18) as srv:
+    # direct=True: on Grace + Blackwell the device gathers the graphs from host memory itself
+    with Server(slots=2, max_batch_nnz=1 << 18, direct_host_access=direct) as srv:
         rids = [None] * len(graphs)
 
         def client(lo, hi):
@@ -71,7 +73,8 @@ def test_memory_budget_evicts_and_refuses():
             assert srv.wait(rid)[0] == ctr.count(big.first_out, big.head)[0]
 
 
-def test_repeats_while_queued_join_the_count():
+@pytest.mark.parametrize("direct", [False, True])
+def test_repeats_while_queued_join_the_count(direct):
     """A request for a key that is still queued or counting is answered by that count; later
     repeats are answered from the resident copy taken on the device from the batch union."""
     big = Graph.rmat(17, 16, seed=9)
@@ -79,7 +82,7 @@ def test_repeats_while_queued_join_the_count():
     with TriangleCounter(0) as ctr:
         want_big = ctr.count(big.first_out, big.head)
         want_small = [ctr.count(g.first_out, g.head) for g in small]
-    with Server(slots=1) as srv:
+    with Server(slots=1, direct_host_access=direct) as srv:
         first = srv.submit(big, key=5)
         again = [srv.submit(big, key=5, borrow=True), srv.submit(None, key=5),
                  srv.submit(big, key=5, per_vertex=False)]
