@@ -51,13 +51,18 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
                                                   u32* __restrict__ dplus, u32* __restrict__ spanning,
                                                   Control* ctl) {
     constexpr int TILE = BLOCK * IPT;
-    __shared__ u64 s_fo[TILE + 2];
+    // Everything inside a tile is addressed relative to its first vertex i0 and first slot j0,
+    // in 32 bits.  s_fo[k] = first_out[i0 + k] - j0 clamped to [0, nslot]: only the first
+    // vertex's start and the last one's end can lie outside the tile.
+    __shared__ u32 s_fo[TILE + 2];
+    __shared__ u32 s_deg[TILE + 2];
     __shared__ u32 s_head[TILE];
     __shared__ u32 s_cnt[TILE + 2];
     __shared__ u32 s_first[TILE + 2];
     __shared__ u32 s_warp[BLOCK / 32];
-    __shared__ u64 s_b[2];
+    __shared__ u64 s_b[3];   // i0, i1, first_out[i0]
     __shared__ u32 s_carry[2];
+    __shared__ u32 s_flags;  // bit 0: the last window vertex's list continues past the tile
 
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 total = n + nnz;
@@ -73,38 +78,62 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     __syncthreads();
     const u64 i0 = s_b[0], i1 = s_b[1];
     const u64 j0 = d0 - i0, j1 = d1 - i1;
+    const u32 nslot = (u32)(j1 - j0);
+    const u32 last = (u32)(i1 - i0);  // window vertices 0..last (last may be n - i0: no vertex)
     const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
     const u32 nfo = (u32)(fo_last - i0 + 1);
     for (u32 k = threadIdx.x; k < nfo; k += BLOCK) {
-        s_fo[k] = fo[i0 + k];
+        const u64 f = fo[i0 + k];
+        s_fo[k] = f < j0 ? 0u : (f > j1 ? nslot : (u32)(f - j0));
         s_cnt[k] = 0;
+        if (k <= last && i0 + k < n) s_deg[k] = deg[i0 + k];
+        if (k == 0) s_b[2] = f;
     }
-    const u32 nslot = (u32)(j1 - j0);
+    if (nfo <= last + 1) s_fo[last + 1] = nslot;  // the window ends at n
     for (u32 k = threadIdx.x; k < nslot; k += BLOCK) s_head[k] = head[j0 + k];
+    if (threadIdx.x == 0) s_flags = (i1 < n && fo[i1 + 1] > j1) ? 1u : 0u;
     __syncthreads();
 
-    // this thread's run of the merge path
-    const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
-    const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
-    const u64 i_start = mp_search_window(s_fo, i0, i0, i1, dt);
-    const u64 j_start = dt - i_start;
+    // this thread's run of the merge path: items t .. te of the tile
+    const u32 t = threadIdx.x * IPT < (u32)(d1 - d0) ? threadIdx.x * IPT : (u32)(d1 - d0);
+    const u32 te = t + IPT < (u32)(d1 - d0) ? t + IPT : (u32)(d1 - d0);
+    u32 i_start;  // largest i in [0, last] with s_fo[i] + i <= t
+    {
+        u32 lo = 0, hi = last;
+        while (lo < hi) {
+            const u32 mid = (lo + hi + 1) >> 1;
+            if (s_fo[mid] + mid <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        i_start = lo;
+    }
+    const u32 j_start = t - i_start;
+    const u32 nv = (u32)(n - i0);  // window vertices that exist: i < nv
 
     u32 own[IPT], yv[IPT];
     bool unsorted = false;
     u32 err = 0;
     {
-        u64 i = i_start, j = j_start;
+        u32 i = i_start, j = j_start;
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             own[k] = NONE;
             yv[k] = 0;
-            if (dt + k < dte) {
-                if (i < n && j < s_fo[i + 1 - i0]) {
-                    own[k] = (u32)(i - i0);
-                    u32 y = s_head[j - j0];
+            if (t + k < te) {
+                if (i < nv && j < s_fo[i + 1]) {
+                    own[k] = i;
+                    const u32 y = s_head[j];
                     yv[k] = y;
-                    if (j + 1 < s_fo[i + 1 - i0]) {
-                        u32 nx = (j + 1 < j1) ? s_head[j + 1 - j0] : __ldg(head + j + 1);
+                    u32 nx = y;
+                    bool has_next = false;
+                    if (j + 1 < s_fo[i + 1]) {
+                        nx = s_head[j + 1];
+                        has_next = true;
+                    } else if (i == last && (s_flags & 1u) && j + 1 == nslot) {
+                        nx = __ldg(head + j0 + nslot);
+                        has_next = true;
+                    }
+                    if (has_next) {
                         if (nx < y) unsorted = true;
                         if (nx == y) err |= DEV_ERR_DUPLICATE;
                     }
@@ -130,7 +159,7 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
             bool out = false;
             if (y >= n) err |= DEV_ERR_ID_RANGE;
             else if ((u64)y == x) err |= DEV_ERR_SELF_LOOP;
-            else out = key_less(s_fo[own[k] + 1] - s_fo[own[k]], x, dy[k], y);
+            else out = key_less(s_deg[own[k]], x, dy[k], y);
             if (own[k] != run_owner) {
                 if (run) atomicAdd(&s_cnt[run_owner], run);
                 run_owner = own[k];
@@ -150,18 +179,19 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     const u32 base = block_exclusive_scan<BLOCK>((u32)__popc(outbits), s_warp, &tot);
 
     // first in-tile slot of every owner: record its scan position; lists wholly inside the
-    // tile publish their out-degree here
+    // tile (every window vertex but possibly the first and the last) publish their out-degree
+    const bool first_whole = s_b[2] >= j0 && (last > 0 || !(s_flags & 1u));
     {
         u32 run = base;
-        u64 j = j_start;
+        u32 j = j_start;
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             if (own[k] == NONE) continue;
             const u32 o = own[k];
-            const u64 first = s_fo[o] > j0 ? s_fo[o] : j0;
-            if (j == first) {
+            if (j == s_fo[o]) {
                 s_first[o] = run;
-                if (s_fo[o] >= j0 && s_fo[o + 1] <= j1) dplus[i0 + o] = s_cnt[o];
+                const bool whole = o == 0 ? first_whole : (o < last || !(s_flags & 1u));
+                if (whole) dplus[i0 + o] = s_cnt[o];
             }
             if (outbits >> k & 1u) ++run;
             ++j;
@@ -171,7 +201,7 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
         s_carry[0] = 0;
         s_carry[1] = 0;
         if (i0 < n) {
-            const u64 a = s_fo[0], b = s_fo[1];
+            const u64 a = fo[i0], b = fo[i0 + 1];
             const u64 lo = a > j0 ? a : j0, hi = b < j1 ? b : j1;
             if (lo < hi && (a < j0 || b > j1)) {
                 s_carry[0] = atomicAdd(&dplus[i0], s_cnt[0]);
@@ -179,9 +209,9 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
             }
         }
         if (i1 != i0 && i1 < n) {
-            const u64 a = s_fo[i1 - i0], b = s_fo[i1 - i0 + 1];
+            const u64 a = fo[i1], b = fo[i1 + 1];
             if (a < j1 && b > j1) {
-                s_carry[1] = atomicAdd(&dplus[i1], s_cnt[i1 - i0]);
+                s_carry[1] = atomicAdd(&dplus[i1], s_cnt[last]);
                 spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)i1;
             }
         }
@@ -193,10 +223,11 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
         for (int k = 0; k < IPT; ++k) {
             if (!(outbits >> k & 1u)) continue;
             const u32 o = own[k];
-            const u64 x = i0 + o;
-            const u32 carry = (x == i0) ? s_carry[0] : (x == i1 ? s_carry[1] : 0u);
-            const u64 pos = (u64)(run - s_first[o]) + carry;
-            headp[oriented_start(s_fo[o], x) + pos] = yv[k];
+            const u32 carry = o == 0 ? s_carry[0] : (o == last ? s_carry[1] : 0u);
+            const u32 pos = run - s_first[o] + carry;
+            // every window vertex after the first starts inside the tile, at j0 + s_fo[o]
+            const u64 fx = o == 0 ? s_b[2] : j0 + s_fo[o];
+            headp[oriented_start(fx, i0 + o) + pos] = yv[k];
             ++run;
         }
     }
