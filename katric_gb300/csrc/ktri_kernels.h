@@ -12,7 +12,7 @@ namespace ktri {
 using u32 = uint32_t;
 using u64 = unsigned long long;
 
-constexpr int ORIENT_BLOCK = 256;
+constexpr int ORIENT_BLOCK = 128;
 constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
