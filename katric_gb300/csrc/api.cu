@@ -209,7 +209,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
                             opt.medium_outdegree, opt.segment, ctl, sms, st);
     if (autom)
-        ktri::launch_order_tiles(fo, head, n, ltiles, &ctl->large_tiles, opt.segment,
+        ktri::launch_order_tiles(fo, head, dplus, n, ltiles, &ctl->large_tiles, opt.segment, false,
                                  reinterpret_cast<u32*>(base + L.thist), lsorted, ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),

@@ -81,11 +81,13 @@ template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
                  u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st);
 
-// Owner tiles reordered by the first vertex their segment streams (*count tiles on the device;
-// hist needs tile_order_scratch_words() u32, sorted the same capacity as tiles).
+// Owner tiles reordered (*count tiles on the device): by the first vertex their segment streams,
+// or with by_degree by their owner's out-degree, largest first.  hist needs
+// tile_order_scratch_words() u32, sorted the same capacity as tiles.
 u64 tile_order_scratch_words();
-void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, const unsigned long long* count,
-                        u32 seg, u32* hist, uint2* sorted, Control* ctl, int num_sms, cudaStream_t st);
+void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n, const uint2* tiles,
+                        const unsigned long long* count, u32 seg, bool by_degree, u32* hist, uint2* sorted,
+                        Control* ctl, int num_sms, cudaStream_t st);
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>

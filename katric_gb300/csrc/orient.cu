@@ -285,18 +285,28 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
 // serves the repeats.  Counts do not depend on the order.
 constexpr u32 TILE_BUCKETS = 4096;
 
-__global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head,
+// Sort key of a tile: the top id bits of the first vertex its segment streams (by_degree =
+// false), or the owner's out-degree, largest first (by_degree = true: longest tiles first).
+__device__ __forceinline__ u32 tile_key(const u64* fo, const u32* head, const u32* dplus, uint2 tl, u32 seg,
+                                        u32 shift, bool by_degree) {
+    u32 key;
+    if (by_degree) {
+        const u32 d = dplus[tl.x];
+        key = d >= TILE_BUCKETS ? 0u : TILE_BUCKETS - 1 - d;
+    } else {
+        key = __ldg(head + fo[tl.x] + (u64)tl.y * seg) >> shift;
+    }
+    return key < TILE_BUCKETS ? key : TILE_BUCKETS - 1;
+}
+
+__global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
                             const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
-                            u32* hist, Control* ctl) {
+                            bool by_degree, u32* hist, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
-    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
-        const uint2 tl = tiles[t];
-        u32 key = __ldg(head + fo[tl.x] + (u64)tl.y * seg) >> shift;
-        if (key >= TILE_BUCKETS) key = TILE_BUCKETS - 1;
-        atomicAdd(&hist[key], 1u);
-    }
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride)
+        atomicAdd(&hist[tile_key(fo, head, dplus, tiles[t], seg, shift, by_degree)], 1u);
 }
 
 __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
@@ -318,17 +328,15 @@ __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
     }
 }
 
-__global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const uint2* __restrict__ tiles,
-                               const unsigned long long* count, u32 seg, u32 shift, u32* cursor,
-                               uint2* __restrict__ sorted, Control* ctl) {
+__global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
+                               const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
+                               bool by_degree, u32* cursor, uint2* __restrict__ sorted, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
         const uint2 tl = tiles[t];
-        u32 key = __ldg(head + fo[tl.x] + (u64)tl.y * seg) >> shift;
-        if (key >= TILE_BUCKETS) key = TILE_BUCKETS - 1;
-        sorted[atomicAdd(&cursor[key], 1u)] = tl;
+        sorted[atomicAdd(&cursor[tile_key(fo, head, dplus, tl, seg, shift, by_degree)], 1u)] = tl;
     }
 }
 
@@ -336,16 +344,18 @@ __global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict
 
 u64 tile_order_scratch_words() { return TILE_BUCKETS; }
 
-void launch_order_tiles(const u64* fo, const u32* head, u64 n, const uint2* tiles, const unsigned long long* count,
-                        u32 seg, u32* hist, uint2* sorted, Control* ctl, int num_sms, cudaStream_t st) {
+void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n, const uint2* tiles,
+                        const unsigned long long* count, u32 seg, bool by_degree, u32* hist, uint2* sorted,
+                        Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u32 bits = 0;
     while ((1ull << bits) < n) ++bits;
     const u32 shift = bits > 12 ? bits - 12 : 0;
     cudaMemsetAsync(hist, 0, sizeof(u32) * TILE_BUCKETS, st);
-    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, count, seg, shift, hist, ctl);
+    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, by_degree, hist, ctl);
     k_tile_scan<<<1, 1024, 0, st>>>(hist, ctl);
-    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, tiles, count, seg, shift, hist, sorted, ctl);
+    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, by_degree, hist, sorted,
+                                                ctl);
 }
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
