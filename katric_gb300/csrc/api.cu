@@ -85,8 +85,8 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
     L.tile_i0 = take(sizeof(u32) * (ktri::base_tiles(n, nnz) + 2));
     u32 grid = 0;
     if (method == KTRI_METHOD_AUTO) {
-        // medium-owner tiles, large-owner tiles, and the large ones reordered
-        L.ltiles = take(sizeof(uint2) * 3 * ktri::large_tile_capacity(n, nnz, small_d, seg));
+        // medium- and large-owner tiles, and both reordered
+        L.ltiles = take(sizeof(uint2) * 4 * ktri::large_tile_capacity(n, nnz, small_d, seg));
         L.thist = take(sizeof(u32) * ktri::tile_order_scratch_words());
         grid = (u32)(sms * 48);  // bound on the small + medium + large persistent grids (occupancy <= 16 each)
     } else {
@@ -211,6 +211,11 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (autom)
         ktri::launch_order_tiles(fo, head, dplus, n, ltiles, &ctl->large_tiles, opt.segment, false,
                                  reinterpret_cast<u32*>(base + L.thist), lsorted, ctl, sms, st);
+    // medium tiles longest owner first, so the warps' last tiles are short ones
+    auto* msorted = autom ? lsorted + tcap : nullptr;
+    if (autom)
+        ktri::launch_order_tiles(fo, head, dplus, n, mtiles, &ctl->medium_tiles, opt.segment, true,
+                                 reinterpret_cast<u32*>(base + L.thist), msorted, ctl, sms, st);
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -222,7 +227,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, lsorted,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, msorted, lsorted,
                                                    opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
                                                    events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
         ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
