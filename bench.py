@@ -49,6 +49,12 @@ METRIC = "edges/s (undirected edges / time of one exact total + per-vertex count
 KERNELS_PER_STEP = 7  # k_prep, k_orient, k_desc, k_count_small, k_count_medium, k_count_large, k_final
 
 
+def kernels_per_count(nnz: int) -> int:
+    """Kernels of one AUTO count: the seven above, plus k_tile_hist / k_tile_scan /
+    k_tile_scatter for the large and the medium tiles from 2^20 adjacency entries on."""
+    return KERNELS_PER_STEP + (6 if nnz >= (1 << 20) else 0)
+
+
 def make_graph(name: str):
     from katric_gb300 import Graph
     w = WORKLOADS[name]
@@ -310,7 +316,7 @@ def run_batch(args):
         "batched_vs_plain": plain_ms / ms,
         "autotune": tune,
         "triangles_total": int(ref_tot.sum().item()),
-        "gpu_launches": (KERNELS_PER_STEP + 1) * args.steps,  # the pipeline's kernels + k_graph_totals per replay
+        "gpu_launches": (kernels_per_count(nnz) + 1) * args.steps,  # the pipeline + k_graph_totals per replay
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -578,7 +584,7 @@ def main():
                                        "dram__bytes_write.sum of the three counting kernels, one capture)"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8)},
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "gpu_launches": kernels_per_count(g.nnz) * args.steps,
         "clocks": clk,
     }
     if not args.no_cpu_baseline and ws == 1:

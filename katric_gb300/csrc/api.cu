@@ -205,17 +205,22 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     auto* mtiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
     const u64 tcap = ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment);
     auto* ltiles = autom ? mtiles + tcap : nullptr;
-    auto* lsorted = autom ? ltiles + tcap : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
                             opt.medium_outdegree, opt.segment, ctl, sms, st);
-    if (autom)
+    // Tile orders (large tiles by the vertex range they stream, for L2 reuse; medium tiles
+    // longest owner first, so the warps' last tiles are short).  Below 2^20 adjacency entries
+    // everything fits L2 and the few tiles are not worth the four extra launches.
+    const bool order = autom && nnz >= (1ull << 20);
+    uint2* lrun = ltiles;
+    uint2* mrun = mtiles;
+    if (order) {
+        lrun = ltiles + tcap;
+        mrun = lrun + tcap;
         ktri::launch_order_tiles(fo, head, dplus, n, ltiles, &ctl->large_tiles, opt.segment, false,
-                                 reinterpret_cast<u32*>(base + L.thist), lsorted, ctl, sms, st);
-    // medium tiles longest owner first, so the warps' last tiles are short ones
-    auto* msorted = autom ? lsorted + tcap : nullptr;
-    if (autom)
+                                 reinterpret_cast<u32*>(base + L.thist), lrun, ctl, sms, st);
         ktri::launch_order_tiles(fo, head, dplus, n, mtiles, &ctl->medium_tiles, opt.segment, true,
-                                 reinterpret_cast<u32*>(base + L.thist), msorted, ctl, sms, st);
+                                 reinterpret_cast<u32*>(base + L.thist), mrun, ctl, sms, st);
+    }
     if (!autom) {
         ktri::launch_sort_lists<OffT>(n, vdesc, headp, reinterpret_cast<u32*>(base + L.mid),
                                       reinterpret_cast<u32*>(base + L.big), reinterpret_cast<u32*>(base + L.scratch),
@@ -227,7 +232,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, msorted, lsorted,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mrun, lrun,
                                                    opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
                                                    events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
         ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
