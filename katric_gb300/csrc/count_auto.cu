@@ -423,17 +423,19 @@ template <int U>
 __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32 d, const u32* keys, u32* hitc, u32 lg,
                                                 const u32* filt, u32 fl, u32* wbuf, int lane, u32 lt_mask) {
     u32 hits = 0, nbuf = 0;
-    for (u32 p0 = 0; p0 < d; p0 += 32 * U) {
+    // a running pointer and a running count of the entries left from this lane's position,
+    // so each load is one instruction with an immediate offset and one compare
+    const u32* lp = lst + lane;
+    int rem = (int)d - lane;
+    for (u32 p0 = 0; p0 < d; p0 += 32 * U, lp += 32 * U, rem -= 32 * U) {
         u32 w[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const u32 p = p0 + 32 * u + lane;
-            w[u] = p < d ? __ldg(lst + p) : EMPTY_KEY;
-        }
+        for (int u = 0; u < U; ++u) w[u] = rem > 32 * u ? __ldg(lp + 32 * u) : EMPTY_KEY;
+        const int left = (int)(d - p0);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            if (p0 + 32 * u >= d) break;
-            const bool maybe = w[u] != EMPTY_KEY && filter_test(filt, fl, w[u]);
+            if (left <= 32 * u) break;
+            const bool maybe = rem > 32 * u && filter_test(filt, fl, w[u]);
             const u32 ball = __ballot_sync(0xFFFFFFFFu, maybe);
             if (maybe) wbuf[nbuf + __popc(ball & lt_mask)] = w[u];
             nbuf += __popc(ball);
