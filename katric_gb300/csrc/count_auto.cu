@@ -435,7 +435,9 @@ __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             if (left <= 32 * u) break;
-            const bool maybe = rem > 32 * u && filter_test(filt, fl, w[u]);
+            // both tests evaluated (no branch): past the list's end w[u] is EMPTY_KEY, a harmless
+            // filter read whose result the range test masks
+            const bool maybe = (rem > 32 * u) & filter_test(filt, fl, w[u]);
             const u32 ball = __ballot_sync(0xFFFFFFFFu, maybe);
             if (maybe) wbuf[nbuf + __popc(ball & lt_mask)] = w[u];
             nbuf += __popc(ball);
@@ -475,7 +477,7 @@ __device__ __forceinline__ u32 lane_stream_short(const uint4* __restrict__ headp
             const u32 wv[4] = {qv[c].x, qv[c].y, qv[c].z, qv[c].w};
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (4 * c + k < (int)dy && filter_test(filt, fl, wv[k])) hits += bucket_probe16(keys, hitc, lg, wv[k]);
+                if ((4 * c + k < (int)dy) & filter_test(filt, fl, wv[k])) hits += bucket_probe16(keys, hitc, lg, wv[k]);
         }
     }
     return hits;
