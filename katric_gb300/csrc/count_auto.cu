@@ -92,6 +92,22 @@ __device__ __forceinline__ u32 bucket_probe16(const u32* keys, u32* hits32, u32 
 }
 
 
+// The same lookup without early exits: one bucket read, a walk along full buckets only when
+// the home bucket is full and holds no w (rare at the tables' load factors), and a predicated
+// hit count, so the lanes of a warp that look up 32 packed filter survivors stay together.
+__device__ __forceinline__ u32 bucket_probe16_flat(const u32* keys, u32* hits32, u32 lg, u32 w) {
+    const u32 nb_mask = (1u << (lg - 2)) - 1;
+    u32 b = bucket_home(w, lg);
+    uint4 q = *reinterpret_cast<const uint4*>(keys + 4 * b);
+    for (u32 it = 0; it < nb_mask && q.w != EMPTY_KEY && q.x != w && q.y != w && q.z != w && q.w != w; ++it) {
+        b = (b + 1) & nb_mask;
+        q = *reinterpret_cast<const uint4*>(keys + 4 * b);
+    }
+    const u32 slot = q.x == w ? 0u : (q.y == w ? 1u : (q.z == w ? 2u : (q.w == w ? 3u : 4u)));
+    if (slot < 4u) hit16(hits32, 4 * b + slot);
+    return slot < 4u ? 1u : 0u;
+}
+
 template <int BLOCK, int IPT, int SD, typename OffT>
 struct SmallLayout {
     static constexpr int TILE = BLOCK * IPT;
@@ -443,7 +459,7 @@ __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32
             nbuf += __popc(ball);
             if (nbuf >= 32) {
                 __syncwarp();
-                hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+                hits += bucket_probe16_flat(keys, hitc, lg, wbuf[lane]);
                 const u32 rest = nbuf - 32;
                 const u32 carry = lane < rest ? wbuf[32 + lane] : 0u;
                 __syncwarp();
@@ -454,7 +470,7 @@ __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32
         }
     }
     __syncwarp();
-    if (lane < nbuf) hits += bucket_probe16(keys, hitc, lg, wbuf[lane]);
+    if (lane < nbuf) hits += bucket_probe16_flat(keys, hitc, lg, wbuf[lane]);
     __syncwarp();
     return hits;
 }
