@@ -294,7 +294,11 @@ typedef struct ktri_server_stats {
     uint64_t submitted, completed, batches, batched_graphs, cache_hits, evictions, resident_graphs, resident_bytes,
         peak_inflight_batches;
     uint64_t coalesced; /* requests answered by the count of an earlier queued request with their key */
-    uint64_t reserved[6];
+    uint64_t pack_us;    /* worker time spent packing batches and enqueueing their copies and counts */
+    uint64_t alloc_us;   /* of pack_us: time spent growing the slots' device and pinned host buffers */
+    uint64_t harvest_us; /* worker time spent reading back results and keeping graphs resident */
+    uint64_t device_us;  /* device time of the batches (first copy to last read-back), summed */
+    uint64_t reserved[2];
 } ktri_server_stats;
 int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out);
 int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,

@@ -69,7 +69,8 @@ class ServerOpts(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "batches", "batched_graphs", "cache_hits",
                                               "evictions", "resident_graphs", "resident_bytes",
-                                              "peak_inflight_batches", "coalesced")] + [("reserved", ctypes.c_uint64 * 6)]
+                                              "peak_inflight_batches", "coalesced", "pack_us", "alloc_us",
+                                              "harvest_us", "device_us")] + [("reserved", ctypes.c_uint64 * 2)]
 
 
 class Tuning(ctypes.Structure):

@@ -68,7 +68,7 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
                    bool force_wide = false, u32 small_d = (u32)ktri::SMALL_D, u32 seg = ktri::LARGE_SEG) {
     Layout L;
     const u64 cap = ktri::oriented_capacity(n, nnz);
-    L.wide = force_wide || cap > 0xFFFFFFFFull;
+    L.wide = force_wide || cap > ktri::NARROW_CAPACITY;
     const int sms = num_sms > 0 ? num_sms : 160;
     size_t off = 0;
     auto take = [&](size_t bytes) {

@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
                 if (s_ko[mid] <= q) lo = mid; else hi = mid - 1;
             }
             const u32 tb = s_tb[lo];
-            const u32 w = __ldg(headp + (u64)s_desc[lo].start + (q - s_ko[lo]));
+            const u32 w = __ldg(headp + list_start(s_desc[lo]) + (q - s_ko[lo]));
             if (!bucket_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
         }
 
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
             if (sel) {
                 const u32 qi = base + __popc(ball & ((1u << lane) - 1));
                 q_y[qi] = yv[k];
-                q_s[qi] = vy[k].start;
+                q_s[qi] = (OffT)list_group(vy[k]);
                 q_m[qi] = (o << 6) | vy[k].d;
                 atomicAdd(&s_bins[vy[k].d], 1u);
             }
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
             const u32* keys = s_keys + (tb >> 5);
             u32* hitc = s_hits + ((tb >> 5) >> 1);  // table offsets are multiples of 4 slots
             const u32 lg = tb & 31u;
-            const u64 q0 = (u64)q_s[qi] >> 2;
+            const u64 q0 = (u64)q_s[qi];
             u32 hits = 0;
             // the list's 16-byte groups are loaded PRE at a time before any probe, so their
             // latencies overlap instead of adding up
@@ -481,7 +481,7 @@ template <typename OffT>
 __device__ __forceinline__ u32 lane_stream_short(const uint4* __restrict__ headp4, const Desc<OffT>& vy,
                                                  const u32* keys, u32* hitc, u32 lg, const u32* filt, u32 fl) {
     const u32 dy = vy.d;
-    const u64 q0 = (u64)vy.start >> 2;
+    const u64 q0 = list_group(vy);
     uint4 qv[LONG_LIST / 4];
 #pragma unroll
     for (int c = 0; c < LONG_LIST / 4; ++c)
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             if (threadIdx.x == 0) {
                 const u32 bytes = ((klen + 3u) & ~3u) * (u32)sizeof(u32);
                 mbar_expect_tx(&s_bar, bytes);
-                bulk_copy_g2s(stage, headp + (u64)dxd.start + c0, bytes, &s_bar);
+                bulk_copy_g2s(stage, headp + list_start(dxd) + c0, bytes, &s_bar);
             }
             const bool arrived = mbar_wait_bounded(&s_bar, phase);
             if (__syncthreads_or(!arrived)) {  // the same decision in every thread
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 qi = __shfl_sync(0xFFFFFFFFu, qi, 0);
                 if (qi >= qn) break;
                 const Desc<OffT> vy = qd[qi];
-                u32 hits = warp_stream_list<U>(headp + (u64)vy.start, vy.d, keys, hitc, lg, filt, fl, wbuf, lane,
+                u32 hits = warp_stream_list<U>(headp + list_start(vy), vy.d, keys, hitc, lg, filt, fl, wbuf, lane,
                                                lt_mask);
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
                 if (lane == 0 && hits) {
@@ -724,7 +724,7 @@ __global__ void __launch_bounds__(BLOCK)
         for (u32 i = lane; i < fwords; i += 32) filt[i] = 0;
         __syncwarp();
         for (u32 q = lane; q < dx; q += 32) {
-            const u32 w = __ldg(headp + (u64)dxd.start + q);
+            const u32 w = __ldg(headp + list_start(dxd) + q);
             if (!bucket_insert(keys, lg, w)) dup = 1;
             const u32 h = filter_bit(w, fl);
             atomicOr(&filt[h >> 5], 1u << (h & 31u));
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(BLOCK)
                 const int src = __ffs(ball) - 1;
                 ball &= ball - 1;
                 const u32 yy = __shfl_sync(0xFFFFFFFFu, y, src);
-                const u64 ys = (u64)__shfl_sync(0xFFFFFFFFu, (unsigned long long)vy.start, src);
+                const u64 ys = (u64)__shfl_sync(0xFFFFFFFFu, (unsigned long long)list_start(vy), src);
                 const u32 yd = __shfl_sync(0xFFFFFFFFu, vy.d, src);
                 u32 hits = warp_stream_list<U>(headp + ys, yd, keys, hitc, lg, filt, fl, wbuf, lane, lt_mask);
                 hits = __reduce_add_sync(0xFFFFFFFFu, hits);
@@ -830,7 +830,7 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
         const Desc<OffT> dv = load_desc(vdesc + v);
         if (lane == 0) oriented += dv.d;
         for (u32 k = lane; k < dv.d; k += 32) {
-            const u32 u = headp[(u64)dv.start + k];
+            const u32 u = headp[list_start(dv) + k];
             const u32 du = load_desc(vdesc + u).d;
             wedge += du;
             isz += (u64)dv.d + du;

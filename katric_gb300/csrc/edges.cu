@@ -46,7 +46,7 @@ __global__ void k_sort_warp(u64 n, const Desc<OffT>* __restrict__ vdesc, u32* __
             }
             continue;
         }
-        u32* p = headp + (u64)d.start;
+        u32* p = headp + list_start(d);
         u32 x = lane < (int)d.d ? p[lane] : EMPTY_KEY;
         const u32 nx = __shfl_down_sync(0xFFFFFFFFu, x, 1);
         const bool bad = lane + 1 < (int)d.d && nx < x;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_sort_block(const Desc<OffT>* __r
     const u64 cnt = *(volatile unsigned long long*)&ctl->sort_mid;
     for (u64 i = blockIdx.x; i < cnt; i += gridDim.x) {
         const Desc<OffT> d = load_desc(vdesc + mid_list[i]);
-        u32* p = headp + (u64)d.start;
+        u32* p = headp + list_start(d);
         u32 P = 1;
         while (P < d.d) P <<= 1;
         if (threadIdx.x == 0) s_bad = 0;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_sort_global(const Desc<OffT>* __
     u32* s = scratch + (u64)blockIdx.x * scratch_per_block;
     for (u64 i = blockIdx.x; i < cnt; i += gridDim.x) {
         const Desc<OffT> d = load_desc(vdesc + big_list[i]);
-        u32* p = headp + (u64)d.start;
+        u32* p = headp + list_start(d);
         u32 P = 1;
         while (P < d.d) P <<= 1;
         if (P > scratch_per_block) {  // cannot happen: out-degree <= sqrt(nnz)
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<Of
         const u64 end = base + EDGE_CHUNK < n ? base + EDGE_CHUNK : n;
         for (u64 v = base; v < end; ++v) {
             const Desc<OffT> dv = load_desc(vdesc + v);
-            const u32* A = headp + (u64)dv.start;
+            const u32* A = headp + list_start(dv);
             u64 tv = 0;
             if (method == KTRI_METHOD_BINARY) {
                 for (u32 k0 = 0; k0 < dv.d; k0 += 32) {
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<Of
                             sink.emit((u32)v, u, w);
                         };
                         const Desc<OffT> du = load_desc(vdesc + u);
-                        c = lane_binary(A, dv.d, headp + (u64)du.start, du.d, cutoff, hit_w, &overflow);
+                        c = lane_binary(A, dv.d, headp + list_start(du), du.d, cutoff, hit_w, &overflow);
                         if (c) atomicAdd(&cnt[u], (u64)c);
                     }
                     tv += c;
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(EDGE_BLOCK) k_count_edges(u64 n, const Desc<Of
                         sink.emit((u32)v, u, w);
                     };
                     const Desc<OffT> du = load_desc(vdesc + u);
-                    const u32* B = headp + (u64)du.start;
+                    const u32* B = headp + list_start(du);
                     u32 c;
                     const bool bs = method == KTRI_METHOD_BINARY_SEARCH ||
                                     (method == KTRI_METHOD_HYBRID && hybrid_use_bsearch(dv.d, du.d, hybrid_scale));
@@ -368,7 +368,7 @@ __global__ void k_export(u64 n, const Desc<OffT>* __restrict__ vdesc, const u32*
     for (u64 v = gw; v < n; v += nwarps) {
         const Desc<OffT> d = load_desc(vdesc + v);
         const u64 o = out_fo[v];
-        for (u32 k = lane; k < d.d; k += 32) out_head[o + k] = headp[(u64)d.start + k];
+        for (u32 k = lane; k < d.d; k += 32) out_head[o + k] = headp[list_start(d) + k];
     }
 }
 

@@ -24,19 +24,33 @@ __host__ __device__ __forceinline__ u64 oriented_start(u64 fo_x, u64 x) { return
 __host__ __device__ __forceinline__ u64 oriented_capacity(u64 n, u64 nnz) { return nnz + 3 * n + 8; }
 
 // Per-vertex descriptor of the oriented out-list: start in the gapped array and length.
+// Every list of the gapped array starts on a 16-byte boundary, so the 32-bit descriptor holds
+// the start in 16-byte groups (4 entries) and addresses gapped arrays of up to 2^34 entries;
+// the 64-bit descriptor holds the start in entries.  list_start / list_group / set_list_start
+// hide the difference.
 template <typename OffT>
 struct Desc;
 template <>
 struct __align__(8) Desc<u32> {
-    u32 start;
+    u32 start;  // in 16-byte groups
     u32 d;
 };
 template <>
 struct __align__(16) Desc<u64> {
-    u64 start;
+    u64 start;  // in entries
     u32 d;
     u32 pad;
 };
+__host__ __device__ __forceinline__ u64 list_start(const Desc<u32>& d) { return (u64)d.start << 2; }
+__host__ __device__ __forceinline__ u64 list_start(const Desc<u64>& d) { return d.start; }
+// the start as an index of 16-byte groups (lists in the gapped array only)
+__host__ __device__ __forceinline__ u64 list_group(const Desc<u32>& d) { return d.start; }
+__host__ __device__ __forceinline__ u64 list_group(const Desc<u64>& d) { return d.start >> 2; }
+// s must be a multiple of 4 for the 32-bit descriptor
+__host__ __device__ __forceinline__ void set_list_start(Desc<u32>& d, u64 s) { d.start = (u32)(s >> 2); }
+__host__ __device__ __forceinline__ void set_list_start(Desc<u64>& d, u64 s) { d.start = s; }
+// Largest gapped array (entries) the 32-bit descriptor addresses.
+constexpr u64 NARROW_CAPACITY = 1ull << 34;
 
 template <typename OffT>
 __device__ __forceinline__ Desc<OffT> load_desc(const Desc<OffT>* p) {

@@ -250,7 +250,7 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
             const u64 a = fo[v], b = fo[v + 1];
             const u32 d = dplus[v];
             Desc<OffT> ds;
-            ds.start = (OffT)oriented_start(a, v);
+            set_list_start(ds, oriented_start(a, v));
             ds.d = d;
             if constexpr (sizeof(OffT) == 8) ds.pad = 0;
             vdesc[v] = ds;

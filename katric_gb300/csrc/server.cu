@@ -33,17 +33,6 @@ using ktri::u64;
 
 namespace {
 
-// Rebase a packed union: graph g's offsets were copied relative to its own start and its
-// ids relative to its own first vertex.
-__global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64* __restrict__ vfirst,
-                         const u64* __restrict__ efirst, u64 num_graphs) {
-    for (u64 g = blockIdx.x; g < num_graphs; g += gridDim.x) {
-        const u64 vb = vfirst[g], ve = vfirst[g + 1], eb = efirst[g], ee = efirst[g + 1];
-        for (u64 v = vb + 1 + threadIdx.x; v <= ve; v += blockDim.x) fo[v] += eb;
-        for (u64 e = eb + threadIdx.x; e < ee; e += blockDim.x) head[e] += (u32)vb;
-    }
-}
-
 // Where the device reads pageable host memory (ATS/HMM over NVLink-C2C on Grace + Blackwell),
 // a batch is gathered straight from the callers' arrays: no host-side packing pass.
 struct GraphSrc {
@@ -63,6 +52,41 @@ __device__ __forceinline__ u64 warp_graph_of(const u64* first, u64 k, u64 x) {
         else hi = mid;
     }
     return lo;
+}
+
+// Rebase a packed union: graph g's offsets were copied relative to its own start and its
+// ids relative to its own first vertex.  The whole grid walks the union (a warp takes 256
+// consecutive elements and finds their graph by binary search), so a large graph is spread
+// over all SMs instead of one block.
+__global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64* __restrict__ vf,
+                         const u64* __restrict__ ef, u64 k, u64 n, u64 nnz) {
+    const int lane = threadIdx.x & 31;
+    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 base = warp * 256; base < nnz; base += nwarps * 256) {
+        u64 g = 0;
+        if (lane == 0) g = warp_graph_of(ef, k, base);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+#pragma unroll 4
+        for (int j = 0; j < 8; ++j) {
+            const u64 e = base + lane + 32 * j;
+            if (e >= nnz) break;
+            while (e >= ef[g + 1]) ++g;
+            head[e] += (u32)vf[g];
+        }
+    }
+    for (u64 base = warp * 256; base < n; base += nwarps * 256) {
+        u64 g = 0;
+        if (lane == 0) g = warp_graph_of(vf, k, base);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+#pragma unroll 4
+        for (int j = 0; j < 8; ++j) {
+            const u64 v = base + lane + 32 * j;
+            if (v >= n) break;
+            while (v >= vf[g + 1]) ++g;
+            fo[v + 1] += ef[g];
+        }
+    }
 }
 
 __global__ void k_gather(const GraphSrc* __restrict__ src, const u64* __restrict__ vf, const u64* __restrict__ ef,
@@ -143,7 +167,7 @@ struct Request {
     bool done = false;
     int status = KTRI_OK;
     uint64_t total = 0;
-    std::vector<uint64_t> pv;
+    std::shared_ptr<std::vector<uint64_t>> pv;  // per-vertex counts (shared with the followers)
     std::vector<Request*> followers;  // later requests for the same key, answered with this one
     bool follower_pv = false;         // a follower wants the per-vertex counts
     bool pv_written = false;          // the batch wrote the per-vertex counts into pv directly
@@ -160,7 +184,8 @@ struct Resident {  // a graph kept on the device with its counts
 struct Slot {
     ktri_ctx* ctx = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr;  // the batch's first copy is enqueued (timing event)
+    cudaEvent_t done = nullptr;   // the batch's last read-back is finished (timing event)
     cudaEvent_t cache_done = nullptr;  // resident copies out of this slot's buffers are finished
     bool busy = false;
     std::vector<Request*> reqs;
@@ -200,6 +225,7 @@ struct ktri_server {
     size_t resident_bytes = 0;
     ktri_server_stats st{};
     int fatal = KTRI_OK;
+    double alloc_s_acc = 0;  // seconds spent in grow() by the worker, moved into st.alloc_us under the lock
 };
 
 namespace {
@@ -252,10 +278,10 @@ void finish(ktri_server* s, Request* r, int status) {
 void serve_resident(ktri_server* s, Request* r, Resident& res) {
     r->total = res.total;
     if (r->want_pv && res.n) {
-        r->pv.resize(res.n);
+        r->pv = std::make_shared<std::vector<uint64_t>>(res.n);
         const char* base = static_cast<const char*>(res.mem);
         const size_t off_pv = al(8 * (res.n + 1)) + al(4 * (res.nnz + 1));
-        cudaMemcpyAsync(r->pv.data(), base + off_pv, 8 * res.n, cudaMemcpyDeviceToHost, s->aux);
+        cudaMemcpyAsync(r->pv->data(), base + off_pv, 8 * res.n, cudaMemcpyDeviceToHost, s->aux);
         cudaStreamSynchronize(s->aux);
     }
     s->lru.erase(res.lru);
@@ -301,8 +327,14 @@ void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 eb
     s->resident.emplace(r->key, res);
 }
 
-int grow(void** p, size_t* have, size_t need, bool host) {
+int grow(ktri_server* s, void** p, size_t* have, size_t need, bool host) {
     if (need <= *have) return KTRI_OK;
+    const double t0 = now_s();
+    struct Charge {
+        ktri_server* s;
+        double t0;
+        ~Charge() { s->alloc_s_acc += now_s() - t0; }
+    } charge{s, t0};
     if (*p) {
         cudaDeviceSynchronize();  // nothing may still read the old buffer
         if (host) cudaFreeHost(*p);
@@ -343,7 +375,7 @@ int launch_batch(ktri_server* s, Slot& sl) {
     sl.off_tot = take(8 * k);
     sl.off_pv = take(8 * (n + 1));
     sl.off_src = take(sizeof(GraphSrc) * (k + 1));
-    int rc = grow(&sl.dev, &sl.dev_bytes, off, false);
+    int rc = grow(s, &sl.dev, &sl.dev_bytes, off, false);
     if (rc) return rc;
     sl.direct = s->pageable && s->opts.direct_host_access;
     // host staging: [fo][head] (staged batches only), [vf][ef][sources], then read-back [tot][pv]
@@ -357,7 +389,7 @@ int launch_batch(ktri_server* s, Slot& sl) {
     const size_t h_vf = htake(8 * (k + 1)), h_ef = htake(8 * (k + 1)), h_src = htake(sizeof(GraphSrc) * (k + 1));
     sl.h_tot = htake(8 * k);
     sl.h_pv = sl.direct ? 0 : htake(8 * (n + 1));
-    rc = grow(&sl.host, &sl.host_bytes, hoff, true);
+    rc = grow(s, &sl.host, &sl.host_bytes, hoff, true);
     if (rc) return rc;
     char* h = static_cast<char*>(sl.host);
     u64* hvf = reinterpret_cast<u64*>(h + h_vf);
@@ -373,12 +405,12 @@ int launch_batch(ktri_server* s, Slot& sl) {
         r->pv_written = false;
         if (sl.direct) {
             if (r->pv_wanted && r->n) {
-                r->pv.resize(r->n);
+                r->pv = std::make_shared<std::vector<uint64_t>>(r->n);
                 r->pv_written = true;
             }
             hsrc[i].fo = reinterpret_cast<const u64*>(r->bfo);
             hsrc[i].head = r->bhead;
-            hsrc[i].pv_out = r->pv_written ? reinterpret_cast<u64*>(r->pv.data()) : nullptr;
+            hsrc[i].pv_out = r->pv_written ? reinterpret_cast<u64*>(r->pv->data()) : nullptr;
         }
     }
     hvf[k] = vb;
@@ -386,6 +418,7 @@ int launch_batch(ktri_server* s, Slot& sl) {
     char* d = static_cast<char*>(sl.dev);
     cudaStream_t st = sl.stream;
     cudaStreamWaitEvent(st, sl.cache_done, 0);  // earlier resident copies read these buffers
+    cudaEventRecord(sl.start, st);
     auto* dfo = reinterpret_cast<u64*>(d + sl.off_fo);
     auto* dhead = reinterpret_cast<u32*>(d + sl.off_head);
     auto* dvf = reinterpret_cast<u64*>(d + sl.off_vf);
@@ -404,7 +437,9 @@ int launch_batch(ktri_server* s, Slot& sl) {
         hfo[0] = 0;
         // pack the graphs into pinned staging in parallel, in pieces of at most 4 MiB so that a
         // large graph is copied by many threads (one host thread copies only ~13 GB/s); ids
-        // are rebased on the device
+        // are rebased on the device.  (Copying large graphs straight from the callers' pageable
+        // arrays with the copy engines measured slower on Grace + Blackwell: the worker thread
+        // blocks in each copy.)
         struct Piece {
             char* dst;
             const char* src;
@@ -427,8 +462,9 @@ int launch_batch(ktri_server* s, Slot& sl) {
             std::memcpy(pieces[(size_t)p].dst, pieces[(size_t)p].src, pieces[(size_t)p].bytes);
         cudaMemcpyAsync(dfo, hfo, 8 * (n + 1), cudaMemcpyHostToDevice, st);
         if (nnz) cudaMemcpyAsync(dhead, hhead, 4 * nnz, cudaMemcpyHostToDevice, st);
-        const unsigned blocks = (unsigned)std::min<u64>(k, 4096);
-        k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k);
+        const u64 warps = (std::max<u64>(n, nnz) + 255) / 256;
+        const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
+        k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k, n, nnz);
     }
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
     ktri_opts o{};
@@ -452,26 +488,43 @@ int launch_batch(ktri_server* s, Slot& sl) {
 
 // Harvest a finished slot (called with the lock held).
 void harvest(ktri_server* s, Slot& sl) {
+    const double t0 = now_s();
+    float dev_ms = 0;
+    if (cudaEventElapsedTime(&dev_ms, sl.start, sl.done) == cudaSuccess) s->st.device_us += (u64)(dev_ms * 1e3);
+    cudaGetLastError();
     int rc = ktri_ctx_check(sl.ctx);
     const char* h = static_cast<const char*>(sl.host);
     const u64* tot = reinterpret_cast<const u64*>(h + sl.h_tot);
     const u64* pv = reinterpret_cast<const u64*>(h + sl.h_pv);
     size_t inflight = 0;
     for (const Slot& o : s->slots) inflight += o.dev_bytes;
+    const int64_t k = (int64_t)sl.reqs.size();
+    if (rc == KTRI_OK && !sl.direct) {
+        // per-vertex counts out of the pinned read-back, one request per host thread
+        std::vector<u64> vfirst((size_t)k);
+        u64 v = 0, pv_bytes = 0;
+        for (int64_t i = 0; i < k; ++i) {
+            vfirst[(size_t)i] = v;
+            v += sl.reqs[(size_t)i]->n;
+            if (sl.reqs[(size_t)i]->want_pv || sl.reqs[(size_t)i]->follower_pv) pv_bytes += 8 * sl.reqs[(size_t)i]->n;
+        }
+#pragma omp parallel for schedule(dynamic, 1) if (k > 1 && pv_bytes > (4u << 20))
+        for (int64_t i = 0; i < k; ++i) {
+            Request* r = sl.reqs[(size_t)i];
+            if (r->want_pv || r->follower_pv)
+                r->pv = std::make_shared<std::vector<uint64_t>>(pv + vfirst[(size_t)i], pv + vfirst[(size_t)i] + r->n);
+        }
+    }
     u64 vb = 0, eb = 0;
-    for (size_t i = 0; i < sl.reqs.size(); ++i) {
-        Request* r = sl.reqs[i];
+    for (int64_t i = 0; i < k; ++i) {
+        Request* r = sl.reqs[(size_t)i];
         if (rc == KTRI_OK) {
             r->total = tot[i];
-            if (sl.direct) {
-                // a follower that asked for counts after the batch started: read them back now
-                if ((r->want_pv || r->follower_pv) && !r->pv_written && r->n) {
-                    r->pv.resize(r->n);
-                    cudaMemcpy(r->pv.data(), static_cast<const char*>(sl.dev) + sl.off_pv + 8 * vb, 8 * r->n,
-                               cudaMemcpyDeviceToHost);
-                }
-            } else if (r->want_pv || r->follower_pv) {
-                r->pv.assign(pv + vb, pv + vb + r->n);
+            // a follower that asked for counts after a direct batch started: read them back now
+            if (sl.direct && (r->want_pv || r->follower_pv) && !r->pv_written && r->n) {
+                r->pv = std::make_shared<std::vector<uint64_t>>(r->n);
+                cudaMemcpy(r->pv->data(), static_cast<const char*>(sl.dev) + sl.off_pv + 8 * vb, 8 * r->n,
+                           cudaMemcpyDeviceToHost);
             }
             keep_resident(s, r, sl, vb, eb, inflight);
         }
@@ -486,6 +539,7 @@ void harvest(ktri_server* s, Slot& sl) {
     cudaEventRecord(sl.cache_done, s->aux);
     sl.reqs.clear();
     sl.busy = false;
+    s->st.harvest_us += (u64)((now_s() - t0) * 1e6);
 }
 
 void worker_main(ktri_server* s) {
@@ -556,8 +610,13 @@ void worker_main(ktri_server* s) {
                 s->st.batches++;
                 s->st.batched_graphs += batch.size();
                 lock.unlock();
+                const double t0 = now_s();
                 const int rc = launch_batch(s, *free_slot);
+                const double t1 = now_s();
                 lock.lock();
+                s->st.pack_us += (u64)((t1 - t0) * 1e6);
+                s->st.alloc_us += (u64)(s->alloc_s_acc * 1e6);
+                s->alloc_s_acc = 0;
                 if (rc) {
                     cudaStreamSynchronize(free_slot->stream);
                     for (Request* r : free_slot->reqs) finish(s, r, rc);
@@ -619,7 +678,8 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
         rc = ktri_ctx_create(device, &sl.ctx);
         if (rc) break;
         cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
-        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        cudaEventCreate(&sl.start);
+        cudaEventCreate(&sl.done);
         cudaEventCreateWithFlags(&sl.cache_done, cudaEventDisableTiming);
     }
     cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
@@ -703,18 +763,27 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
 int ktri_server_wait(ktri_server* s, uint64_t request_id, uint64_t* total, uint64_t* per_vertex_out,
                      double* latency_s) {
     if (!s) return KTRI_ERR_INVALID_ARGUMENT;
-    std::unique_lock<std::mutex> lock(s->mu);
-    auto it = s->requests.find(request_id);
-    if (it == s->requests.end()) return KTRI_ERR_INVALID_ARGUMENT;
-    Request* r = it->second.get();
-    s->cv_done.wait(lock, [&] { return r->done; });
+    std::unique_ptr<Request> r;
+    {
+        std::unique_lock<std::mutex> lock(s->mu);
+        auto it = s->requests.find(request_id);
+        if (it == s->requests.end()) return KTRI_ERR_INVALID_ARGUMENT;
+        Request* p = it->second.get();
+        s->cv_done.wait(lock, [&] { return p->done; });
+        r = std::move(it->second);
+        s->requests.erase(it);
+    }
+    // The worker finished with the request before marking it done (under the lock), so its
+    // counts are read back without holding the lock: large copies do not stall the worker.
     const int status = r->status;
     if (status == KTRI_OK) {
         if (total) *total = r->total;
-        if (per_vertex_out && r->want_pv && r->n) std::memcpy(per_vertex_out, r->pv.data(), 8 * r->n);
+        if (per_vertex_out && r->want_pv && r->n) {
+            if (r->pv) std::memcpy(per_vertex_out, r->pv->data(), 8 * r->n);
+            else std::memset(per_vertex_out, 0, 8 * r->n);
+        }
     }
     if (latency_s) *latency_s = r->t_done - r->t_submit;
-    s->requests.erase(it);
     return status;
 }
 
@@ -745,6 +814,7 @@ int ktri_server_destroy(ktri_server* s) {
         if (sl.ctx) ktri_ctx_destroy(sl.ctx);  // before the stream it last ran on goes away
         if (sl.dev) cudaFree(sl.dev);
         if (sl.host) cudaFreeHost(sl.host);
+        if (sl.start) cudaEventDestroy(sl.start);
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.cache_done) cudaEventDestroy(sl.cache_done);
         if (sl.stream) cudaStreamDestroy(sl.stream);

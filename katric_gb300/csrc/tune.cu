@@ -7,7 +7,8 @@
 // Search: the library default (KTRI_METHOD_AUTO with bins 32 / 256, segment 1024) is timed
 // first; then the reference's strategies (hybrid first; merge, binary search and binary only
 // when hybrid comes within 1.5x of the best); then, if an AUTO configuration is best, one pass
-// of coordinate descent over small_outdegree, medium_outdegree and segment.
+// of coordinate descent over small_outdegree, medium_outdegree and segment.  A candidate
+// replaces the best configuration so far only when it is more than 2 % faster.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,9 +19,13 @@
 #include <vector>
 
 #include "ktri.h"
+
 #include "ktri_internal.h"
 
 namespace {
+
+// Relative gain a candidate must show over the best configuration so far to replace it.
+constexpr double kMinGain = 0.02;
 
 using u64 = unsigned long long;
 
@@ -194,6 +199,9 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                 res.candidates++;
                 return KTRI_OK;
             };
+            // a candidate replaces the incumbent only when it is faster by more than the timing
+            // noise (and the difference between the tuning sample and the full input)
+            auto clearly_faster = [](double t, double incumbent) { return t < (1.0 - kMinGain) * incumbent; };
             Cand def;
             double t = 0;
             rc = timed(def, &best_ms);
@@ -204,7 +212,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
             hy.method = KTRI_METHOD_HYBRID;
             rc = timed(hy, &t);
             if (rc) break;
-            if (t < best_ms) {
+            if (clearly_faster(t, best_ms)) {
                 best = hy;
                 best_ms = t;
             }
@@ -214,7 +222,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                     c.method = m;
                     rc = timed(c, &t);
                     if (rc) break;
-                    if (t < best_ms) {
+                    if (clearly_faster(t, best_ms)) {
                         best = c;
                         best_ms = t;
                     }
@@ -228,7 +236,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                     if (c.medium < s) c.medium = s;
                     rc = timed(c, &t);
                     if (rc) break;
-                    if (t < best_ms) {
+                    if (clearly_faster(t, best_ms)) {
                         best = c;
                         best_ms = t;
                     }
@@ -239,7 +247,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                     c.medium = std::max(m, c.small);
                     rc = timed(c, &t);
                     if (rc) break;
-                    if (t < best_ms) {
+                    if (clearly_faster(t, best_ms)) {
                         best = c;
                         best_ms = t;
                     }
@@ -250,7 +258,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                     c.seg = g;
                     rc = timed(c, &t);
                     if (rc) break;
-                    if (t < best_ms) {
+                    if (clearly_faster(t, best_ms)) {
                         best = c;
                         best_ms = t;
                     }

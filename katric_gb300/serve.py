@@ -62,7 +62,7 @@ class Server:
             n, want, _keep = self._meta.pop(rid)
         total = ctypes.c_uint64(0)
         lat = ctypes.c_double(0)
-        pv = np.zeros(max(1, n), dtype=np.uint64) if want else None
+        pv = np.empty(max(1, n), dtype=np.uint64) if want else None
         rc = self._L.ktri_server_wait(self._h, rid, ctypes.byref(total), pv.ctypes.data if pv is not None else None,
                                       ctypes.byref(lat))
         _native.check(rc)
