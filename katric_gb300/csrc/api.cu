@@ -65,7 +65,7 @@ u64 isqrt_ceil(u64 x) {
 
 // Workspace of one count.  num_sms = 0 sizes the grids for the largest supported part.
 Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs, bool internal_cnt,
-                   bool force_wide = false, u32 small_d = (u32)ktri::SMALL_D, u32 seg = ktri::LARGE_SEG) {
+                   bool force_wide = false, u32 small_d = (u32)ktri::SMALL_D_LOW, u32 seg = ktri::LARGE_SEG) {
     Layout L;
     const u64 cap = ktri::oriented_capacity(n, nnz);
     L.wide = force_wide || cap > ktri::NARROW_CAPACITY;
@@ -235,7 +235,7 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
         KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mrun, lrun,
                                                    opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
                                                    events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
-        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
+        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, opt.small_outdegree), d_total, ctl, st);
     } else {
         const int grid = ktri::count_grid_edges(sms);
         ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
@@ -279,7 +279,7 @@ int check_common(ktri_ctx* ctx, const void* fo, const void* head, u64 n, u64 nnz
     if (opt.method < KTRI_METHOD_AUTO || opt.method > KTRI_METHOD_HYBRID)
         return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "unknown intersection method");
     if (opt.small_outdegree < 1 || opt.small_outdegree > (u32)ktri::SMALL_D)
-        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "small_outdegree must be in 1..32");
+        return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "small_outdegree must be in 1..48");
     if (opt.medium_outdegree < opt.small_outdegree || opt.medium_outdegree > (u32)ktri::MEDIUM_D)
         return set_error(ctx, KTRI_ERR_INVALID_ARGUMENT, "medium_outdegree must be in small_outdegree..256");
     if (opt.segment < ktri::MIN_SEG || opt.segment > ktri::LARGE_SEG || (opt.segment & (opt.segment - 1)))
@@ -375,18 +375,18 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
     auto* partials = reinterpret_cast<u64*>(base + L.partials);
     auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
     auto* mtiles = reinterpret_cast<uint2*>(base + L.ltiles);
-    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, (u32)ktri::SMALL_D, ktri::LARGE_SEG);
+    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, (u32)ktri::SMALL_D_LOW, ktri::LARGE_SEG);
     // the control block (counters, error word) must start at zero; k_prep zeroes the
     // out-degrees and per-vertex counts; every other region is fully written before it is read
     if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return KTRI_ERR_CUDA;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
     ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
-    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, (u32)ktri::SMALL_D, (u32)ktri::MEDIUM_D,
+    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, (u32)ktri::SMALL_D_LOW, (u32)ktri::MEDIUM_D,
                             ktri::LARGE_SEG, ctl, sms, st);
-    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, (u32)ktri::SMALL_D,
+    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, (u32)ktri::SMALL_D_LOW,
                                       ktri::LARGE_SEG, cnt, partials, ctl, sms, st, nullptr, nullptr) != cudaSuccess)
         return KTRI_ERR_CUDA;
-    ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms), d_total, ctl, st);
+    ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, (u32)ktri::SMALL_D_LOW), d_total, ctl, st);
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
     u32 herr = 0;
     if (cudaMemcpyAsync(&herr, &ctl->err, sizeof(u32), cudaMemcpyDeviceToHost, st) != cudaSuccess) return KTRI_ERR_CUDA;
@@ -1149,8 +1149,10 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
         return cuda_fail(ctx, e, "cudaMalloc(plan workspace)");
     }
     // occupancy queries happen once, outside the capture
-    (void)ktri::count_grid_auto<u32>(ctx->num_sms);
-    (void)ktri::count_grid_auto<u64>(ctx->num_sms);
+    for (u32 sd : {(u32)ktri::SMALL_D_LOW, (u32)ktri::SMALL_D}) {
+        (void)ktri::count_grid_auto<u32>(ctx->num_sms, sd);
+        (void)ktri::count_grid_auto<u64>(ctx->num_sms, sd);
+    }
     cudaStream_t cs = nullptr;
     cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     char* base = static_cast<char*>(p->ws);

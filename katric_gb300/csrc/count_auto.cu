@@ -859,20 +859,20 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
 // ---- launchers ------------------------------------------------------------------------
 
 namespace {
-template <typename OffT>
-using SmallL = SmallLayout<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>;
+template <int SD, typename OffT>
+using SmallL = SmallLayout<SMALL_BLOCK, SMALL_IPT, SD, OffT>;
 template <typename OffT>
 using LargeL = LargeLayout<LARGE_BLOCK, LARGE_CAP, OffT>;
 using MediumL = MediumLayout<MEDIUM_BLOCK>;
 
-template <typename OffT>
+template <int SD, typename OffT>
 int occupancy_small() {
     static int occ = -1;
     if (occ < 0) {
-        auto kern = k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<OffT>::bytes);
+        auto kern = k_count_small<SMALL_BLOCK, SMALL_IPT, SD, OffT>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<SD, OffT>::bytes);
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<OffT>::bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<SD, OffT>::bytes);
         occ = o > 0 ? o : 1;
     }
     return occ;
@@ -904,8 +904,9 @@ int occupancy_large() {
 }  // namespace
 
 template <typename OffT>
-int count_grid_small(int num_sms) {
-    return num_sms * occupancy_small<OffT>();
+int count_grid_small(int num_sms, u32 small_d) {
+    return num_sms * (small_d <= (u32)SMALL_D_LOW ? occupancy_small<SMALL_D_LOW, OffT>()
+                                                  : occupancy_small<SMALL_D, OffT>());
 }
 template <typename OffT>
 int count_grid_medium(int num_sms) {
@@ -916,8 +917,9 @@ int count_grid_large(int num_sms) {
     return num_sms * occupancy_large<OffT>();
 }
 template <typename OffT>
-int count_grid_auto(int num_sms) {
-    return count_grid_small<OffT>(num_sms) + count_grid_medium<OffT>(num_sms) + count_grid_large<OffT>(num_sms);
+int count_grid_auto(int num_sms, u32 small_d) {
+    return count_grid_small<OffT>(num_sms, small_d) + count_grid_medium<OffT>(num_sms) +
+           count_grid_large<OffT>(num_sms);
 }
 
 template <typename OffT>
@@ -925,13 +927,16 @@ cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, co
                               const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
                               u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
                               cudaEvent_t after_small, cudaEvent_t after_large) {
-    const int gs = count_grid_small<OffT>(num_sms);
+    const int gs = count_grid_small<OffT>(num_sms, small_d);
     const int gm = count_grid_medium<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
-    k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT>
-        <<<gs, SMALL_BLOCK, SmallL<OffT>::bytes, st>>>(fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials,
-                                                       ctl);
+    if (small_d <= (u32)SMALL_D_LOW)
+        k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D_LOW, OffT><<<gs, SMALL_BLOCK, SmallL<SMALL_D_LOW, OffT>::bytes, st>>>(
+            fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials, ctl);
+    else
+        k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT><<<gs, SMALL_BLOCK, SmallL<SMALL_D, OffT>::bytes, st>>>(
+            fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials, ctl);
     if (after_small) cudaEventRecord(after_small, st);
     k_count_medium<MEDIUM_BLOCK, OffT>
         <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, seg, cnt, partials + gs, ctl);
@@ -961,14 +966,14 @@ void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, cons
     k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp, ctl);
 }
 
-template int count_grid_small<u32>(int);
-template int count_grid_small<u64>(int);
+template int count_grid_small<u32>(int, u32);
+template int count_grid_small<u64>(int, u32);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
 template int count_grid_medium<u32>(int);
 template int count_grid_medium<u64>(int);
-template int count_grid_auto<u32>(int);
-template int count_grid_auto<u64>(int);
+template int count_grid_auto<u32>(int, u32);
+template int count_grid_auto<u64>(int, u32);
 template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
                                             const uint2*, const uint2*, u32, u32,
                                             u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);

@@ -16,7 +16,9 @@ constexpr int ORIENT_BLOCK = 128;
 constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
-constexpr int SMALL_D = 32;          // out-degree bound of the tile kernel's owners
+constexpr int SMALL_D = 48;          // largest out-degree bound of the tile kernel's owners
+constexpr int SMALL_D_LOW = 32;      // bounds up to this run the tile kernel's instantiation for 32
+                                     // (five blocks per SM; the one for 48 fits four)
 constexpr int MEDIUM_D = 256;        // out-degree bound of the warp-per-tile kernel's owners
 constexpr int MEDIUM_BLOCK = 256;
 constexpr int LARGE_BLOCK = 256;
@@ -91,13 +93,13 @@ void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n,
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
-int count_grid_small(int num_sms);
+int count_grid_small(int num_sms, u32 small_d);
 template <typename OffT>
 int count_grid_medium(int num_sms);
 template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
-int count_grid_auto(int num_sms);  // small + medium + large
+int count_grid_auto(int num_sms, u32 small_d);  // small + medium + large, for this small-owner bound
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
                               const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,

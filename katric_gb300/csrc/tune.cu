@@ -230,7 +230,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                 if (rc) break;
             }
             if (best.method == KTRI_METHOD_AUTO) {
-                for (uint32_t s : {8u, 16u, 32u}) {
+                for (uint32_t s : {8u, 16u, 32u, 48u}) {
                     Cand c = best;
                     c.small = s;
                     if (c.medium < s) c.medium = s;

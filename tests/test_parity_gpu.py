@@ -139,7 +139,7 @@ def test_many_components_mixed(counter, oracle):
 
 
 @pytest.mark.parametrize("small,medium,segment", [(1, 1, 64), (8, 64, 128), (16, 256, 256), (32, 32, 512),
-                                                   (32, 128, 1024), (4, 200, 64)])
+                                                   (32, 128, 1024), (4, 200, 64), (48, 48, 1024), (40, 256, 256)])
 def test_bin_thresholds_and_segments(counter, oracle, small, medium, segment):
     """Every owner-bin split and tile segment gives the same counts (the autotuner's space)."""
     graphs = [Graph.rmat(14, 16, seed=4), Graph.rgg2d(1 << 13, 24.0, seed=5)]
@@ -151,7 +151,7 @@ def test_bin_thresholds_and_segments(counter, oracle, small, medium, segment):
         assert t == total and np.array_equal(p, pv), (small, medium, segment)
 
 
-@pytest.mark.parametrize("bad", [dict(small_outdegree=33), dict(small_outdegree=16, medium_outdegree=8),
+@pytest.mark.parametrize("bad", [dict(small_outdegree=49), dict(small_outdegree=16, medium_outdegree=8),
                                  dict(medium_outdegree=257), dict(segment=100), dict(segment=32),
                                  dict(segment=2048)])
 def test_bad_bin_options(counter, bad):
