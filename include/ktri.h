@@ -51,8 +51,7 @@ typedef struct ktri_opts {
     uint32_t struct_size;          /* sizeof(ktri_opts); 0 is read as "all defaults" */
     int32_t intersection_method;   /* KTRI_METHOD_* */
     uint32_t small_outdegree;      /* owners with out-degree <= this use the tile kernel: 1..48 (0 = default 32;
-                                      above 32 the kernel fits four instead of five blocks per SM, which pays
-                                      off on graphs of average degree above ~40) */
+                                      bounds above 32 pay off on graphs of average degree above ~40) */
     uint32_t collect_stats;        /* 1: also compute wedge_checks / intersection work counters */
     uint64_t binary_intersection_cutoff; /* Config::binary_intersection_cutoff (config.h:173), default 1000 */
     double hybrid_cutoff_scale;    /* Config::hybrid_cutoff_scale (config.h:174), default 1.0 */

@@ -124,7 +124,7 @@ struct SmallLayout {
     static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * (TBL / 2));
     static constexpr size_t off_qs = align16(off_qy + sizeof(u32) * TILE);
     static constexpr size_t off_qm = align16(off_qs + sizeof(OffT) * TILE);
-    static constexpr size_t off_ord = align16(off_qm + sizeof(u32) * TILE);
+    static constexpr size_t off_ord = align16(off_qm + sizeof(unsigned short) * TILE);
     static constexpr size_t bytes = align16(off_ord + sizeof(unsigned short) * TILE);
 };
 
@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
     constexpr int TILE = L::TILE;
     constexpr int WPT = L::WPT;
     static_assert(SD < 64, "list length is packed in 6 bits");
+    static_assert(TILE + 2 <= 1024, "window owner index is packed in 10 bits");
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned short* s_fo = reinterpret_cast<unsigned short*>(smem + L::off_fo);
     Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
     u32* s_hits = reinterpret_cast<u32*>(smem + L::off_hits);
     u32* q_y = reinterpret_cast<u32*>(smem + L::off_qy);
     OffT* q_s = reinterpret_cast<OffT*>(smem + L::off_qs);
-    u32* q_m = reinterpret_cast<u32*>(smem + L::off_qm);
+    unsigned short* q_m = reinterpret_cast<unsigned short*>(smem + L::off_qm);  // (owner << 6) | list length
     unsigned short* q_ord = reinterpret_cast<unsigned short*>(smem + L::off_ord);
     __shared__ u32 s_warp[BLOCK / 32];
     __shared__ u64 s_red[BLOCK / 32];
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
                 const u32 qi = base + __popc(ball & ((1u << lane) - 1));
                 q_y[qi] = yv[k];
                 q_s[qi] = (OffT)list_group(vy[k]);
-                q_m[qi] = (o << 6) | vy[k].d;
+                q_m[qi] = (unsigned short)((o << 6) | vy[k].d);
                 atomicAdd(&s_bins[vy[k].d], 1u);
             }
         }

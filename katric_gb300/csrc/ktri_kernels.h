@@ -17,8 +17,8 @@ constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_IPT = 3;
 constexpr int SMALL_D = 48;          // largest out-degree bound of the tile kernel's owners
-constexpr int SMALL_D_LOW = 32;      // bounds up to this run the tile kernel's instantiation for 32
-                                     // (five blocks per SM; the one for 48 fits four)
+constexpr int SMALL_D_LOW = 32;      // bounds up to this run the tile kernel's instantiation for 32,
+                                     // the others the one for SMALL_D (more table and bin space)
 constexpr int MEDIUM_D = 256;        // out-degree bound of the warp-per-tile kernel's owners
 constexpr int MEDIUM_BLOCK = 256;
 constexpr int LARGE_BLOCK = 256;
