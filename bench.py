@@ -104,6 +104,12 @@ class ClockSampler:
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # a region shorter than nvidia-smi's start-up and sampling interval got no sample: take the
+        # first one, right after the region
+        after = not self.lines
+        t0 = time.perf_counter()
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 2.0:
+            time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -124,8 +130,11 @@ class ClockSampler:
             for nm, val in zip(names, parts[5:9]):
                 if val.lower() == "active":
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+               "reasons": sorted(reasons), "samples": len(sm)}
+        if after:
+            out["note"] = "timed region shorter than the sampling interval: sampled right after it"
+        return out
 
 
 def measured_traffic(workload: str):

@@ -17,8 +17,10 @@ def graph_mix(count, seed):
 
 @pytest.mark.parametrize("direct", [False, True])
 def test_results_alone_equal_results_in_the_mix(direct):
+    # besides the mix: a larger RMAT graph, an edgeless graph and a graph without vertices
     graphs = graph_mix(90, seed=31) + [Graph.rmat(15, 16, seed=3), Graph(np.zeros(5, np.uint64),
-                                                                          np.zeros(0, np.uint32))]
+                                                                          np.zeros(0, np.uint32)),
+                                       Graph(np.zeros(1, np.uint64), np.zeros(0, np.uint32))]
     with TriangleCounter(0) as ctr:
         alone = [ctr.count(g.first_out, g.head) for g in graphs]
     # direct=True: on Grace + Blackwell the device gathers the graphs from host memory itself
@@ -29,7 +31,8 @@ def test_results_alone_equal_results_in_the_mix(direct):
             for i in range(lo, hi):
                 rids[i] = srv.submit(graphs[i], key=1000 + i, borrow=(i % 2 == 0))
 
-        threads = [threading.Thread(target=client, args=(k * 23, min(len(graphs), (k + 1) * 23))) for k in range(4)]
+        per = (len(graphs) + 3) // 4
+        threads = [threading.Thread(target=client, args=(k * per, min(len(graphs), (k + 1) * per))) for k in range(4)]
         for t in threads:
             t.start()
         for t in threads:
