@@ -352,6 +352,47 @@ int grow(ktri_server* s, void** p, size_t* have, size_t need, bool host) {
     return KTRI_OK;
 }
 
+// Offsets of a batch of k graphs (n vertices, nnz entries) in a slot's device buffer and in
+// its pinned host staging.
+struct SlotLayout {
+    size_t fo = 0, head = 0, vf = 0, ef = 0, tot = 0, pv = 0, src = 0, dev_bytes = 0;
+    size_t h_fo = 0, h_head = 0, h_vf = 0, h_ef = 0, h_src = 0, h_tot = 0, h_pv = 0, host_bytes = 0;
+};
+
+SlotLayout slot_layout(u64 n, u64 nnz, u64 k, bool direct) {
+    SlotLayout L;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t at = off;
+        off = al(off + b);
+        return at;
+    };
+    L.fo = take(8 * (n + 1));
+    L.head = take(4 * (nnz + 1));
+    L.vf = take(8 * (k + 1));
+    L.ef = take(8 * (k + 1));
+    L.tot = take(8 * k);
+    L.pv = take(8 * (n + 1));
+    L.src = take(sizeof(GraphSrc) * (k + 1));
+    L.dev_bytes = off;
+    // host staging: [fo][head] (staged batches only), [vf][ef][sources], then read-back [tot][pv]
+    size_t hoff = 0;
+    auto htake = [&](size_t b) {
+        size_t at = hoff;
+        hoff = al(hoff + b);
+        return at;
+    };
+    L.h_fo = direct ? 0 : htake(8 * (n + 1));
+    L.h_head = direct ? 0 : htake(4 * (nnz + 1));
+    L.h_vf = htake(8 * (k + 1));
+    L.h_ef = htake(8 * (k + 1));
+    L.h_src = htake(sizeof(GraphSrc) * (k + 1));
+    L.h_tot = htake(8 * k);
+    L.h_pv = direct ? 0 : htake(8 * (n + 1));
+    L.host_bytes = hoff;
+    return L;
+}
+
 // Pack the slot's requests and launch their count.  Called without the lock.
 int launch_batch(ktri_server* s, Slot& sl) {
     const u64 k = sl.reqs.size();
@@ -362,34 +403,21 @@ int launch_batch(ktri_server* s, Slot& sl) {
     }
     sl.n_total = n;
     sl.nnz_total = nnz;
-    size_t off = 0;
-    auto take = [&](size_t b) {
-        size_t at = off;
-        off = al(off + b);
-        return at;
-    };
-    sl.off_fo = take(8 * (n + 1));
-    sl.off_head = take(4 * (nnz + 1));
-    sl.off_vf = take(8 * (k + 1));
-    sl.off_ef = take(8 * (k + 1));
-    sl.off_tot = take(8 * k);
-    sl.off_pv = take(8 * (n + 1));
-    sl.off_src = take(sizeof(GraphSrc) * (k + 1));
-    int rc = grow(s, &sl.dev, &sl.dev_bytes, off, false);
-    if (rc) return rc;
     sl.direct = s->pageable && s->opts.direct_host_access;
-    // host staging: [fo][head] (staged batches only), [vf][ef][sources], then read-back [tot][pv]
-    size_t hoff = 0;
-    auto htake = [&](size_t b) {
-        size_t at = hoff;
-        hoff = al(hoff + b);
-        return at;
-    };
-    const size_t h_fo = sl.direct ? 0 : htake(8 * (n + 1)), h_head = sl.direct ? 0 : htake(4 * (nnz + 1));
-    const size_t h_vf = htake(8 * (k + 1)), h_ef = htake(8 * (k + 1)), h_src = htake(sizeof(GraphSrc) * (k + 1));
-    sl.h_tot = htake(8 * k);
-    sl.h_pv = sl.direct ? 0 : htake(8 * (n + 1));
-    rc = grow(s, &sl.host, &sl.host_bytes, hoff, true);
+    const SlotLayout L = slot_layout(n, nnz, k, sl.direct);
+    sl.off_fo = L.fo;
+    sl.off_head = L.head;
+    sl.off_vf = L.vf;
+    sl.off_ef = L.ef;
+    sl.off_tot = L.tot;
+    sl.off_pv = L.pv;
+    sl.off_src = L.src;
+    int rc = grow(s, &sl.dev, &sl.dev_bytes, L.dev_bytes, false);
+    if (rc) return rc;
+    const size_t h_fo = L.h_fo, h_head = L.h_head, h_vf = L.h_vf, h_ef = L.h_ef, h_src = L.h_src;
+    sl.h_tot = L.h_tot;
+    sl.h_pv = L.h_pv;
+    rc = grow(s, &sl.host, &sl.host_bytes, L.host_bytes, true);
     if (rc) return rc;
     char* h = static_cast<char*>(sl.host);
     u64* hvf = reinterpret_cast<u64*>(h + h_vf);
@@ -683,6 +711,22 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
         cudaEventCreateWithFlags(&sl.cache_done, cudaEventDisableTiming);
     }
     cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+    if (rc == KTRI_OK) {
+        // Reserve every slot's union buffer and pinned staging for a full batch (max_batch_nnz
+        // entries over max_batch_nnz / 8 vertices) when all slots together take at most a
+        // quarter of the memory budget: the first large batches then find their buffers ready
+        // instead of growing them (a device synchronisation and a pinned allocation each) while
+        // requests wait.  Batches with more vertices still grow them.
+        const u64 nnz_r = s->opts.max_batch_nnz, n_r = nnz_r / 8;
+        const SlotLayout R = slot_layout(n_r, nnz_r, s->opts.max_batch_graphs, s->pageable && s->opts.direct_host_access);
+        if ((R.dev_bytes + R.dev_bytes / 4) * s->slots.size() <= s->opts.memory_budget / 4) {
+            for (Slot& sl : s->slots)
+                if (grow(s, &sl.dev, &sl.dev_bytes, R.dev_bytes, false) != KTRI_OK ||
+                    grow(s, &sl.host, &sl.host_bytes, R.host_bytes, true) != KTRI_OK)
+                    break;  // not fatal: batches grow the buffers as they need them
+        }
+        s->alloc_s_acc = 0;  // set-up time is not the requests' allocation time
+    }
     cudaSetDevice(prev);
     if (rc) {
         for (Slot& sl : s->slots)
