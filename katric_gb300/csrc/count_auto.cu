@@ -14,7 +14,8 @@
 //
 // Three kernels split the owners by out-degree (the bounds are runtime options, at most
 // SMALL_D and MEDIUM_D):
-//   k_count_small: owners with out-degree <= small_outdegree.  Merge-path tiles over the
+//   k_count_small: owners with out-degree <= small_outdegree (instantiated for bounds up to
+//     SMALL_D_LOW and up to SMALL_D, both five blocks per SM).  Merge-path tiles over the
 //     adjacency (as in orientation) give every block the same number of slots; the tables of
 //     all owners in a tile live side by side in shared memory.  Selected edges are queued,
 //     counting-sorted by streamed-list length so that the lanes of a warp carry equal work,
