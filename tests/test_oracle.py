@@ -118,3 +118,38 @@ def test_per_vertex_brute_force(oracle):
         t, pv, _ = oracle.count(fo, heads, method=method, num_threads=2)
         assert t == total
         assert (pv == expected).all()
+
+
+def test_work_counters_match_their_definition(oracle):
+    """The oracle's work counters, which give the roofline's algorithmic bytes, recomputed from
+    the (degree, id) orientation in numpy: wedge_checks = sum over oriented edges (v,u) of
+    |N+(u)| and intersection_size_local = sum of |N+(v)| + |N+(u)|
+    (cetric_edge_iterator.h:279-281).  A sample stride of 1 counts the whole graph."""
+    rng = np.random.default_rng(11)
+    n, m = 300, 2500
+    edges = set()
+    while len(edges) < m:
+        a, b = (int(x) for x in rng.integers(0, n, 2))
+        if a != b:
+            edges.add((min(a, b), max(a, b)))
+    adj = [[] for _ in range(n)]
+    for a, b in edges:
+        adj[a].append(b)
+        adj[b].append(a)
+    fo = np.zeros(n + 1, dtype=np.uint64)
+    fo[1:] = np.cumsum([len(a) for a in adj])
+    head = np.array([u for a in adj for u in a], dtype=np.uint32)
+    deg = np.array([len(a) for a in adj])
+    key = lambda v: (deg[v], v)  # degree_outward, distributed_graph.h:148-163
+    dplus = np.array([sum(1 for u in adj[v] if key(v) < key(u)) for v in range(n)])
+    wedges = isz = 0
+    for v in range(n):
+        for u in adj[v]:
+            if key(v) < key(u):
+                wedges += int(dplus[u])
+                isz += int(dplus[v] + dplus[u])
+    for method in METHODS:
+        t, _, st = oracle.count(fo, head, method=method, num_threads=2)
+        assert st["wedge_checks"] == wedges and st["intersection_size_local"] == isz, method
+        ts, sst = oracle.count_sampled(fo, head, 1, method=method, num_threads=2)
+        assert ts == t and sst["wedge_checks"] == wedges, method
