@@ -588,6 +588,9 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
             }
             const bool arrived = mbar_wait_bounded(&s_bar, phase);
             if (__syncthreads_or(!arrived)) {  // the same decision in every thread
+                // give the copy in flight a second bounded wait, so that it does not land in
+                // shared memory after the block has left; then report the timeout
+                (void)mbar_wait_bounded(&s_bar, phase);
                 timed_out = true;
                 break;
             }
