@@ -9,7 +9,11 @@ out-list compaction, owner-side hash intersection, per-vertex counts and the u64
   python bench.py --impl reference ...   # the CPU restatement of the reference's path
 
 Prints one JSON line (rank 0).  metric: undirected edges per second (value: device-resident
-inputs; e2e: host buffers through the public API, copies inside the timed region).
+inputs; e2e: host buffers through the public API, copies inside the timed region).  At one GPU
+the default run also measures the batched form (8192 graphs in one captured plan against the
+plain per-graph loop) and the served form (a 60 s Poisson stream against the continuous-batching
+server, then the same requests at saturation against the plain loop), and adds their numbers
+to the same line under "batched" and "served".
 """
 from __future__ import annotations
 
@@ -65,14 +69,48 @@ def make_graph(name: str):
     return Graph.gnm(w["n"], w["m"], w["seed"])
 
 
-def workload_config(name: str, g) -> dict:
+def make_graph_cpu(name: str):
+    """The same graph through the generators built without CUDA (oracle/libgraphgen.so), for the
+    CPU arm: (first_out u64, head u32)."""
+    from oracle import graphgen
+    w = WORKLOADS[name]
+    if w["kind"] == "rmat":
+        return graphgen.rmat(w["scale"], w["edge_factor"], 0.57, 0.19, 0.19, w["seed"])
+    if w["kind"] == "rgg2d":
+        return graphgen.rgg2d(w["n"], w["avg_degree"], w["seed"])
+    return graphgen.gnm(w["n"], w["m"], w["seed"])
+
+
+def csr_sha256(first_out, head) -> str:
+    """SHA-256 of the CSR bytes (u64 first_out, then u32 head): both arms print it, so equal
+    digests show that they counted the same graph."""
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(first_out, dtype=np.uint64).view(np.uint8).data)
+    h.update(np.ascontiguousarray(head, dtype=np.uint32).view(np.uint8).data)
+    return h.hexdigest()
+
+
+def workload_config(name: str, n: int, nnz: int, sha: str) -> dict:
+    """The config dict both arms print (identical for the same workload and graph)."""
     w = dict(WORKLOADS[name])
-    cfg = {"workload": name, "n": g.n, "m_undirected": g.m, "nnz": g.nnz}
+    cfg = {"workload": name, "n": n, "m_undirected": nnz // 2, "nnz": nnz}
     cfg.update({k: v for k, v in w.items() if k != "kind"})
     cfg["generator"] = w["kind"]
     if w["kind"] == "rmat":
         cfg["abcd"] = [0.57, 0.19, 0.19, 0.05]
+    cfg["csr_sha256"] = sha
+    cfg["l2"] = "inputs larger than L2 (CSR %.2f GB vs 129 MB L2)" % ((8 * (n + 1) + 4 * nnz) / 1e9)
     return cfg
+
+
+def fixture(name: str) -> dict | None:
+    """The oracle's full-size record of a workload (tests/golden/fullsize.json), if any."""
+    p = os.path.join(ROOT, "tests", "golden", "fullsize.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(name)
 
 
 class ClockSampler:
@@ -183,51 +221,78 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_baseline_sample(g, target_s: float = 15.0, threads: int | None = None) -> dict:
-    """The oracle (CPU restatement of the reference path) on all host cores, on a bounded
-    sample: full preprocessing, local phase over a 1/stride sample of tail vertices."""
+def cpu_baseline_sample(first_out, head, target_s: float = 12.0, slices: int = 20, threads: int | None = None) -> dict:
+    """The oracle (CPU restatement of the reference path, merge strategy) on all host cores, on
+    a bounded sample: pieces of a full count (a hash slice of the vertices each: their lists
+    oriented and id-sorted, then the node-parallel local phase over them as tails), timed
+    until about target_s seconds of CPU work; value = the pieces' edges / their time."""
     from oracle import oracle as O
     threads = threads or (os.cpu_count() or 1)
-    stride = 1
-    probe_stride = 4096
-    _, st = O.count_sampled(g.first_out, g.head, probe_stride, num_threads=threads)
-    est_full = st["local_phase_s"] * probe_stride
-    if est_full > target_s:
-        stride = int(min(probe_stride, max(1, round(est_full / target_s))))
-    _, st = O.count_sampled(g.first_out, g.head, stride, num_threads=threads)
-    pre = st["orientation_s"] + st["sorting_s"]
-    local_est = st["local_phase_s"] * stride
-    t = pre + local_est
-    return {"value": g.m / t, "unit": "edges/s", "cores": threads, "kind": "port",
-            "sample": (f"oracle (C/OpenMP restatement of run_shmem) on the same graph: full orientation+sort "
-                       f"({pre:.2f} s), merge local phase over a 1/{stride} hash sample of tail vertices "
-                       f"({st['local_phase_s']:.2f} s, scaled x{stride}); estimated full time {t:.2f} s"),
-            "est_seconds": t}
+    sc = O.SlicedCount(first_out, head, slices, num_threads=threads)
+    adj, secs, k = 0, 0.0, 0
+    while k < slices and (k == 0 or secs < target_s):
+        t0 = time.perf_counter()
+        _, a, _ = sc.run(k)
+        secs += time.perf_counter() - t0
+        adj += a
+        k += 1
+    return {"value": (adj / 2) / secs, "unit": "edges/s", "cores": threads, "kind": "port",
+            "sample": (f"oracle (C/OpenMP restatement of run_shmem, merge) on the same graph: {k} of {slices} hash "
+                       f"slices of the vertices, each timed as orientation + id sort of its lists and the local "
+                       f"phase over its tail vertices; {adj // 2} of {len(head) // 2} edges in {secs:.2f} s")}
 
 
 def run_reference_arm(args):
+    """The reference's CPU path, restated (the oracle, merge strategy as in run_shmem's default),
+    on all host cores.  The timed steps together are exactly one full count: step i orients and
+    sorts the lists of hash slice i of the vertices and runs the local phase over its tail
+    vertices, for slices = steps, so the K timed steps cover every vertex once.  The input is
+    built by the generators compiled without CUDA (oracle/libgraphgen.so)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    g = make_graph(args.workload)
+    from oracle import oracle as O
+    fo, hd = make_graph_cpu(args.workload)
+    n, nnz = len(fo) - 1, len(hd)
+    cfg = workload_config(args.workload, n, nnz, csr_sha256(fo, hd))
     threads = os.cpu_count() or 1
-    times = []
-    cb = None
+    slices = args.ref_slices or args.steps
+    t0 = time.perf_counter()
+    sc = O.SlicedCount(fo, hd, slices, num_threads=threads)
+    setup_s = time.perf_counter() - t0
+    times, adj, tri = [], 0, 0
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline_sample(g, target_s=args.ref_step_seconds, threads=threads)
-        if i >= args.warmup:
-            times.append(cb["est_seconds"])
-    t = statistics.median(times)
-    v = g.m / t
+        j = i - args.warmup
+        s = j % slices  # warm-up steps run the last slices, the timed ones 0, 1, ...
+        t0 = time.perf_counter()
+        t, a, _ = sc.run(s)
+        dt = time.perf_counter() - t0
+        if j >= 0:
+            times.append(dt)
+            adj += a
+            tri += t
+    full = args.steps % slices == 0
+    secs = sum(times)
+    v = (adj / 2) / secs
+    fx = fixture(args.workload)
     line = {"metric": METRIC, "value": v, "unit": "edges/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)", "impl": "reference",
-            "config": workload_config(args.workload, g),
+            "warmup": args.warmup, "ms_per_step": secs * 1e3 / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator, no dataset)",
+            "impl": "reference", "config": cfg,
+            "count_s": secs * slices / args.steps,
+            "step_s": {"min": min(times), "median": statistics.median(times), "max": max(times)},
             "cpu_baseline": {"value": v, "unit": "edges/s", "cores": threads, "kind": "port",
-                             "sample": cb["sample"]},
+                             "sample": (f"full count timed in {args.steps} pieces ({slices} hash slices of the "
+                                        f"vertices: orientation + id sort of each slice's lists, then the local "
+                                        f"phase over its tail vertices){'' if full else '; partial coverage'}; "
+                                        f"whole-graph preprocessing before the steps, untimed: {setup_s:.2f} s")},
             "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference (C++17, TBB/MPI/Boost/sparsehash, un-vendored graph-io) cannot be built here; "
-                    "this is the oracle restatement of its path on all host cores"}
+                    "this is the oracle restatement of its path (merge intersection) on all host cores"}
+    if full:
+        line["triangles"] = tri * slices // args.steps
+        if fx and "total" in fx:
+            line["triangles_match_oracle_fixture"] = line["triangles"] == fx["total"]
     print(json.dumps(line), flush=True)
 
 
@@ -239,12 +304,16 @@ def tune_cache_path() -> str:
     return path
 
 
-def run_batch(args):
+def run_batch(args, steps: int, warmup: int, plain_passes: int = 3) -> dict:
     """Batched workload: one captured plan (CUDA graph) over the packed union of all graphs,
-    against the plain loop of one device entry-point call per graph, both timed here."""
+    against the plain loop of one device entry-point call per graph (median of plain_passes
+    passes), both timed here.  The per-graph totals are compared with the oracle's record of
+    this batch when tests/golden/fullsize.json holds one."""
+    import hashlib
     import torch
-    from katric_gb300 import Batch, Config, TriangleCounter
-    w = WORKLOADS[args.workload]
+    from katric_gb300 import Batch, TriangleCounter
+    name = args.workload if WORKLOADS[args.workload]["kind"] == "batch" else "batch8192"
+    w = WORKLOADS[name]
     t0 = time.perf_counter()
     b = Batch.generate(w["graphs"], w["log2_n"][0], w["log2_n"][1], w["degree"][0], w["degree"][1], w["seed"])
     gen_s = time.perf_counter() - t0
@@ -266,10 +335,11 @@ def run_batch(args):
                               cache_path=tune_cache_path(), stream=stream.cuda_stream)
     tune.update({"sample_graphs": ks, "tune_s": round(time.perf_counter() - t0, 2),
                  "chosen": {"intersection_method": conf.intersection_method, "small_outdegree": conf.small_outdegree,
-                            "medium_outdegree": conf.medium_outdegree, "segment": conf.segment}})
+                            "medium_outdegree": conf.medium_outdegree, "segment": conf.segment,
+                            "tile_order": conf.tile_order}})
     plan = ctr.plan_batch(fo.data_ptr(), hd.data_ptr(), n, nnz, gf.data_ptr(), k, tot.data_ptr(), pv.data_ptr(),
                           conf)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plan.launch(stream.cuda_stream)
     plan.check()
     ref_tot = tot.clone()
@@ -278,14 +348,21 @@ def run_batch(args):
     clocks.start()
     torch.cuda.synchronize()
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         plan.launch(stream.cuda_stream)
     ev1.record(stream)
     torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = ev0.elapsed_time(ev1) / steps
     clk = clocks.stop()
     plan.check()
     assert torch.equal(tot, ref_tot)
+    totals = ref_tot.cpu().numpy().astype("<u8")
+    fx = fixture(name)
+    pinned = None
+    if fx and fx.get("graphs") == k:
+        pinned = (hashlib.sha256(totals.view(np.uint8).data).hexdigest() == fx["totals_sha256"] and
+                  hashlib.sha256(pv.cpu().numpy().astype("<u8").view(np.uint8).data).hexdigest() ==
+                  fx["per_vertex_sha256"])
     # plain loop: one ktri_count_csr_device call per graph on per-graph device CSRs
     gfo = b.graph_first.astype(np.int64)
     ufo = b.union.first_out.astype(np.int64)
@@ -297,38 +374,40 @@ def run_batch(args):
         per.append((f.contiguous(), h.contiguous(), int(e - a), int(ufo[e] - ufo[a])))
     out_t = torch.zeros(k, dtype=torch.int64, device=dev)
     out_pv = torch.zeros(int(max(p[2] for p in per)) + 1, dtype=torch.int64, device=dev)
-    cfg = conf
 
     def plain_pass():
         for g, (f, h, gn, gnnz) in enumerate(per):
-            ctr.count_device(f.data_ptr(), h.data_ptr(), gn, gnnz, out_t[g:g + 1].data_ptr(), out_pv.data_ptr(), cfg,
+            ctr.count_device(f.data_ptr(), h.data_ptr(), gn, gnnz, out_t[g:g + 1].data_ptr(), out_pv.data_ptr(), conf,
                              stream=stream.cuda_stream)
 
     plain_pass()  # warm-up (grows the workspace to the largest graph)
     ctr.check()
     assert torch.equal(out_t, ref_tot), "plain loop and batch disagree"
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    plain_pass()
-    ctr.check()
-    plain_ms = (time.perf_counter() - t1) * 1e3
-    line = {
-        "metric": METRIC + "; batched workload", "value": b.union.m / (ms / 1e3), "unit": "edges/s",
-        "graphs_per_s": k / (ms / 1e3), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic (seeded generators)",
-        "config": {"workload": args.workload, "graphs": k, "n_total": n, "m_total": b.union.m, "seed": w["seed"],
-                   "log2_n": list(w["log2_n"]), "degree": list(w["degree"]), "generation_s": round(gen_s, 2),
-                   "path": "one captured plan (CUDA graph) over the packed union"},
-        "plain_loop": {"ms": plain_ms, "graphs_per_s": k / (plain_ms / 1e3), "edges_per_s": b.union.m / (plain_ms / 1e3),
+    plain = []
+    for _ in range(plain_passes):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        plain_pass()
+        ctr.check()
+        plain.append((time.perf_counter() - t1) * 1e3)
+    plain_ms = statistics.median(plain)
+    del per, fo, hd, pv
+    ctr.close()
+    return {
+        "workload": name, "graphs": k, "n_total": n, "m_total": b.union.m, "seed": w["seed"],
+        "generation_s": round(gen_s, 1),
+        "path": "one captured plan (CUDA graph) over the packed union, device-resident inputs",
+        "ms_per_batch": ms, "steps": steps, "warmup": warmup,
+        "graphs_per_s": k / (ms / 1e3), "edges_per_s": b.union.m / (ms / 1e3),
+        "plain_loop": {"ms_median": plain_ms, "ms_passes": plain, "graphs_per_s": k / (plain_ms / 1e3),
                        "path": "ktri_count_csr_device per graph, one stream, device-resident inputs"},
         "batched_vs_plain": plain_ms / ms,
         "autotune": tune,
-        "triangles_total": int(ref_tot.sum().item()),
-        "gpu_launches": (kernels_per_count(nnz) + 1) * args.steps,  # the pipeline + k_graph_totals per replay
+        "triangles_total": int(totals.sum()),
+        "totals_match_oracle_fixture": pinned,
+        "gpu_launches": (kernels_per_count(nnz) + 1) * steps,  # the pipeline + k_graph_totals per replay
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
 
 
 def serve_requests(w, seconds, rate):
@@ -353,12 +432,11 @@ def serve_requests(w, seconds, rate):
     return arrivals, reqs, specs
 
 
-def run_serve(args):
+def run_serve(args, passes: int = 3) -> dict:
     """Served workload: Poisson arrivals replayed against the continuous-batching server (p50/p99
     latency, achieved graphs/s); then the same request list at saturation against the server
-    and against the plain loop (one synchronous ktri_count_csr_ctx call per request)."""
-    import threading
-    import katric_gb300
+    and against the plain loop (one synchronous ktri_count_csr_ctx call per request), each
+    `passes` times (medians reported)."""
     from katric_gb300 import Config, Server, TriangleCounter
     from katric_gb300.graph import generate_many
     w = WORKLOADS["serve"]
@@ -401,36 +479,41 @@ def run_serve(args):
     with Server(memory_budget=w["budget"], direct_host_access=args.serve_direct) as srv:
         wall, lat = replay(srv, paced=True)
         st = srv.stats()
-    with Server(memory_budget=w["budget"], direct_host_access=args.serve_direct) as srv:
-        sat_wall, _ = replay(srv, paced=False)
-        sat_st = srv.stats()
+    sat_walls, sat_st = [], None
+    for _ in range(passes):
+        with Server(memory_budget=w["budget"], direct_host_access=args.serve_direct) as srv:
+            sw, _ = replay(srv, paced=False)
+            sat_walls.append(sw)
+            sat_st = srv.stats()
     ctr = TriangleCounter(0)
     for g in req_graph[:3]:
         ctr.count(g.first_out, g.head, per_vertex=True)  # warm-up
-    t1 = time.perf_counter()
-    for g in req_graph:
-        ctr.count(g.first_out, g.head, Config(), per_vertex=True)
-    plain_wall = time.perf_counter() - t1
+    plain_walls = []
+    for _ in range(passes):
+        t1 = time.perf_counter()
+        for g in req_graph:
+            ctr.count(g.first_out, g.head, Config(), per_vertex=True)
+        plain_walls.append(time.perf_counter() - t1)
+    ctr.close()
+    sat_wall, plain_wall = statistics.median(sat_walls), statistics.median(plain_walls)
     lat_ms = np.array(lat) * 1e3
     k = len(reqs)
-    line = {
-        "metric": "served graphs/s and p50/p99 latency (exact total + per-vertex counts per request)",
-        "value": k / wall, "unit": "graphs/s", "n_gpus": 1, "steps": k, "warmup": 0,
-        "ms_per_step": wall * 1e3 / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32", "data": "synthetic (seeded generators)",
-        "config": {"workload": "serve", "rate_per_s": w["rate"], "seconds": seconds, "requests": k,
-                   "host_copies": "device reads host memory where it can" if args.serve_direct else "pinned staging",
-                   "distinct_graphs": len(specs), "m_total": m_total, "median_m": w["median_m"], "sigma": w["sigma"],
-                   "repeat": w["repeat"], "memory_budget": w["budget"], "generation_s": round(gen_s, 1)},
+    return {
+        "workload": "serve", "rate_per_s": w["rate"], "seconds": seconds, "requests": k,
+        "host_copies": "device reads host memory where it can" if args.serve_direct else "pinned staging",
+        "distinct_graphs": len(specs), "m_total": m_total, "median_m": w["median_m"], "sigma": w["sigma"],
+        "repeat": w["repeat"], "memory_budget": w["budget"], "generation_s": round(gen_s, 1),
+        "paced": {"graphs_per_s": k / wall, "wall_s": wall},
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
                        "mean": float(lat_ms.mean()), "max": float(lat_ms.max())},
         "server": st,
-        "saturation": {"graphs_per_s": k / sat_wall, "edges_per_s": m_total / sat_wall, "server": sat_st},
+        "saturation": {"graphs_per_s": k / sat_wall, "edges_per_s": m_total / sat_wall, "wall_s_passes": sat_walls,
+                       "server": sat_st},
         "plain_loop": {"graphs_per_s": k / plain_wall, "edges_per_s": m_total / plain_wall,
+                       "wall_s_passes": plain_walls,
                        "path": "ktri_count_csr_ctx per request (host buffers, synchronous, no resident graphs)"},
         "served_vs_plain_at_saturation": plain_wall / sat_wall,
     }
-    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -441,7 +524,10 @@ def main():
     ap.add_argument("--workload", default="rmat24", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-slices", type=int, default=0,
+                    help="reference arm: hash slices of a count (default: --steps, so the timed steps are one count)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched and served measurements of the default run")
     ap.add_argument("--serve-seconds", type=float, default=0.0, help="duration of the served stream (default 60)")
     ap.add_argument("--serve-direct", action="store_true",
                     help="let the GPU read and write the requests' host memory directly where it can")
@@ -451,11 +537,25 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args)
         return
-    if WORKLOADS[args.workload]["kind"] in ("batch", "serve"):
+    kind = WORKLOADS[args.workload]["kind"]
+    if kind in ("batch", "serve"):
         # the batched and served forms measure one GPU; under torchrun rank 0 runs them
         if dist_env()[1] != 0:
             return
-        (run_batch if WORKLOADS[args.workload]["kind"] == "batch" else run_serve)(args)
+        if kind == "batch":
+            r = run_batch(args, args.steps, args.warmup)
+            head = {"metric": METRIC + "; batched workload", "value": r["edges_per_s"], "unit": "edges/s",
+                    "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_batch"],
+                    "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}
+        else:
+            r = run_serve(args)
+            head = {"metric": "served graphs/s and p50/p99 latency (exact total + per-vertex counts per request)",
+                    "value": r["paced"]["graphs_per_s"], "unit": "graphs/s", "n_gpus": 1, "steps": r["requests"],
+                    "warmup": 0, "ms_per_step": r["paced"]["wall_s"] * 1e3 / r["requests"]}
+        head.update({"higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                     "data": "synthetic (seeded generators)", "config": {"workload": args.workload}})
+        head.update({k: v for k, v in r.items() if k not in head})
+        print(json.dumps(head), flush=True)
         return
 
     import torch
@@ -471,6 +571,7 @@ def main():
     torch.cuda.set_device(dev)
 
     g = make_graph(args.workload)
+    csr_sha = csr_sha256(g.first_out, g.head)
     ctr = TriangleCounter(dev)
     fo_d = torch.from_numpy(g.first_out.view(np.int64)).to(f"cuda:{dev}")
     hd_d = torch.from_numpy(g.head.view(np.int32)).to(f"cuda:{dev}")
@@ -547,9 +648,16 @@ def main():
         e2e_step()
     e2e_steps = max(3, min(args.steps, 10))
     barrier()
+    split = {"h2d": [], "d2h": [], "call": [], "orient": [], "count": []}
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
+        st = ctr.stats()  # device-side split of the call (the library's events)
+        split["h2d"].append(st.ms_h2d)
+        split["d2h"].append(st.ms_d2h)
+        split["call"].append(st.ms_call)
+        split["orient"].append(st.ms_orient)
+        split["count"].append(st.ms_count)
     t1 = time.perf_counter()
     barrier()
     e2e_ms = (t1 - t0) * 1e3 / e2e_steps
@@ -576,8 +684,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator, no dataset)",
-        "config": dict(workload_config(args.workload, g), parallelism=f"replicas x{ws}",
-                       l2="inputs larger than L2 (CSR %.2f GB vs 129 MB L2)" % ((8 * (n + 1) + 4 * g.nnz) / 1e9)),
+        "config": workload_config(args.workload, n, g.nnz, csr_sha),
+        "parallelism": f"replicas x{ws}",
         "triangles": total_ref,
         "hbm_gbs_algorithmic": b_total / (ms / 1e3) / 1e9,
         "phases_ms": {"orient": statistics.mean(orient_ms), "count_small": statistics.mean(small_ms),
@@ -592,14 +700,31 @@ def main():
                      "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read.sum + "
                                        "dram__bytes_write.sum of the three counting kernels, one capture)"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8)},
+                "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8),
+                "split_ms": {k: statistics.median(v) for k, v in split.items()},
+                "split_note": "device time inside ktri_count_csr_ctx (library events): h2d = first input copy to "
+                              "last piece of head landed (orientation runs on the pieces already in), orient = "
+                              "orientation phase incl. waiting for pieces, count = intersection phase, d2h = "
+                              "read-back of total + per-vertex counts, call = all of it"},
         "gpu_launches": kernels_per_count(g.nnz) * args.steps,
         "clocks": clk,
     }
+    fx = fixture(args.workload)
+    if fx and fx.get("csr_sha256") == csr_sha:
+        # the oracle's full count of this same graph (tests/golden/fullsize.json)
+        line["triangles_match_oracle_fixture"] = total_ref == fx["total"]
     if not args.no_cpu_baseline and ws == 1:
-        cb = cpu_baseline_sample(g)
-        cb.pop("est_seconds", None)
-        line["cpu_baseline"] = cb
+        line["cpu_baseline"] = cpu_baseline_sample(g.first_out, g.head)
+    if ws == 1 and not args.no_forms and args.workload == "rmat24":
+        # the batched and served forms of the same metric family, on the same GPU
+        del fo_h, hd_h, pv_h, fo_d, hd_d, pv_d, pv_ref
+        ctr.close()
+        torch.cuda.empty_cache()
+        line["batched"] = run_batch(args, args.steps, args.warmup)
+        torch.cuda.empty_cache()
+        line["served"] = run_serve(args)
+        line["batched_vs_plain"] = line["batched"]["batched_vs_plain"]
+        line["served_vs_plain_at_saturation"] = line["served"]["served_vs_plain_at_saturation"]
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

@@ -62,8 +62,21 @@ typedef struct ktri_opts {
                                       (0 = default 256) */
     uint32_t segment;              /* adjacency slots per owner tile of those two kernels: a power of two
                                       in 64..1024 (0 = default 1024) */
-    uint32_t reserved[5];
+    uint32_t copy_wait_polls;      /* bound on the polls of the large-owner kernel's first wait for each
+                                      bulk copy into shared memory (0 = default 2^22).  A wait that runs
+                                      out makes the call fail with KTRI_ERR_TIMEOUT and a total of 0.
+                                      KTRI_COPY_WAIT_NONE gives up at once (tests of that path). */
+    uint32_t tile_order;           /* order in which the medium- and large-owner kernels take their tiles:
+                                      0 (default) large tiles by the first vertex they stream (tiles that run
+                                      together read nearby out-lists), medium tiles longest owner first;
+                                      KTRI_TILE_ORDER_COST both by the entries each tile streams, heaviest first
+                                      (the reference's DPD edge cost, cost_function.h:287-376, per tile) */
+    uint32_t reserved[3];
 } ktri_opts;
+
+#define KTRI_TILE_ORDER_COST 1u
+
+#define KTRI_COPY_WAIT_NONE 0xFFFFFFFFu
 
 /* Counters of the last run on a context, named after the reference's Statistics fields
  * (include/cetric/statistics.h:193-199) where one exists. */
@@ -82,7 +95,13 @@ typedef struct ktri_run_stats {
     float ms_total;                   /* device time of the whole call */
     float ms_count_small;             /* AUTO: device time of the small-owner tile kernel */
     float ms_count_large;             /* AUTO: device time of the large-owner vertex kernel */
-    uint32_t reserved[3];
+    float ms_h2d;                     /* host-buffer calls: device time from the first input copy until the
+                                         last piece of head has landed (orientation overlaps it) */
+    float ms_d2h;                     /* host-buffer calls: device time of the read-back of the results */
+    float ms_call;                    /* host-buffer calls: device time of the whole call, copies included */
+    uint64_t streamed_chunked;        /* entries the AUTO kernels stream, counted once per owner-table chunk
+                                         that streams them (collect_stats); above streamed_entries only when
+                                         some owner has more than 2048 out-neighbours */
 } ktri_run_stats;
 
 typedef struct ktri_ctx ktri_ctx;
@@ -137,8 +156,9 @@ int ktri_ctx_check(ktri_ctx* ctx);
  * ktri_workspace_bytes(n, nnz, KTRI_METHOD_AUTO) <= 64 MiB (about 600 000 vertices with 16
  * adjacency entries each); larger graphs return KTRI_ERR_UNSUPPORTED before anything is
  * launched.
- * The first call on a device looks up the array's device address (once per device, with
- * that device current); make that first call before any stream capture.  All calls on a
+ * The first call on a device looks up the array's device address (with that device current;
+ * again whenever the calling thread's CUDA context has changed, e.g. after cudaDeviceReset);
+ * make that first call before any stream capture.  All calls on a
  * device share the one array and leave the last call's contents in it; calls whose work
  * overlaps on the GPU race on it, so serialise them.  Runs on `stream` and returns when that
  * work is done, with KTRI_ERR_INVALID_CSR for invalid input found on the device. */
@@ -254,7 +274,7 @@ typedef struct ktri_tuning {
     uint32_t small_outdegree, medium_outdegree, segment;
     uint32_t from_cache;         /* 1: read from the cache file, nothing timed */
     uint32_t candidates;         /* configurations timed */
-    uint32_t reserved0;
+    uint32_t tile_order;         /* the chosen ktri_opts.tile_order */
     double ms;                   /* device time of one count with the chosen configuration */
     double default_ms;           /* the same with the library defaults (0 when read from the cache) */
     char signature[96];          /* the shape class */

@@ -20,6 +20,8 @@ ERR_IO = -7
 ERR_NO_DEVICE = -8
 
 METHOD_AUTO, METHOD_MERGE, METHOD_BINARY_SEARCH, METHOD_BINARY, METHOD_HYBRID = 0, 1, 2, 3, 4
+COPY_WAIT_NONE = 0xFFFFFFFF  # KTRI_COPY_WAIT_NONE
+TILE_ORDER_COST = 1  # KTRI_TILE_ORDER_COST
 
 ERROR_NAMES = {
     ERR_INVALID_ARGUMENT: "invalid argument",
@@ -50,7 +52,9 @@ class Opts(ctypes.Structure):
         ("force_wide_offsets", ctypes.c_uint32),
         ("medium_outdegree", ctypes.c_uint32),
         ("segment", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 5),
+        ("copy_wait_polls", ctypes.c_uint32),
+        ("tile_order", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 3),
     ]
 
 
@@ -82,7 +86,7 @@ class Tuning(ctypes.Structure):
         ("segment", ctypes.c_uint32),
         ("from_cache", ctypes.c_uint32),
         ("candidates", ctypes.c_uint32),
-        ("reserved0", ctypes.c_uint32),
+        ("tile_order", ctypes.c_uint32),
         ("ms", ctypes.c_double),
         ("default_ms", ctypes.c_double),
         ("signature", ctypes.c_char * 96),
@@ -105,7 +109,10 @@ class RunStats(ctypes.Structure):
         ("ms_total", ctypes.c_float),
         ("ms_count_small", ctypes.c_float),
         ("ms_count_large", ctypes.c_float),
-        ("reserved", ctypes.c_uint32 * 3),
+        ("ms_h2d", ctypes.c_float),
+        ("ms_d2h", ctypes.c_float),
+        ("ms_call", ctypes.c_float),
+        ("streamed_chunked", ctypes.c_uint64),
     ]
 
 

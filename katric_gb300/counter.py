@@ -57,6 +57,9 @@ class Config:
     small_outdegree: int = 0    # owner bins of the "auto" kernels (0 = library default; see ktri_opts)
     medium_outdegree: int = 0
     segment: int = 0
+    copy_wait_polls: int = 0    # bound on the large-owner kernel's first bulk-copy wait (0 = default;
+                                # COPY_WAIT_NONE gives up at once, for tests of the timeout path)
+    tile_order: int = 0         # 0: tiles by locality (default); 1: by streamed work, heaviest first
 
     def opts(self) -> _native.Opts:
         o = _native.Opts()
@@ -72,6 +75,8 @@ class Config:
         o.binary_intersection_cutoff = self.binary_intersection_cutoff
         o.hybrid_cutoff_scale = self.hybrid_cutoff_scale
         o.force_wide_offsets = 1 if self.force_wide_offsets else 0
+        o.copy_wait_polls = self.copy_wait_polls
+        o.tile_order = self.tile_order
         return o
 
 
@@ -305,7 +310,8 @@ class TriangleCounter:
                                           ctypes.byref(res), stream or None))
         name = {v: k for k, v in METHOD_BY_NAME.items() if "_" not in k}[res.intersection_method]
         tuned = dataclasses.replace(conf, intersection_method=name, small_outdegree=res.small_outdegree,
-                                    medium_outdegree=res.medium_outdegree, segment=res.segment)
+                                    medium_outdegree=res.medium_outdegree, segment=res.segment,
+                                    tile_order=res.tile_order)
         info = {"from_cache": bool(res.from_cache), "candidates": int(res.candidates), "ms": float(res.ms),
                 "default_ms": float(res.default_ms), "signature": res.signature.decode()}
         return tuned, info

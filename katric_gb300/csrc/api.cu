@@ -1,4 +1,5 @@
 // C ABI: contexts, workspace management and the counting entry points.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <fcntl.h>
 #include <sys/stat.h>
@@ -7,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -33,6 +35,13 @@ struct ktri_ctx {
     std::string last_error;
     ktri_run_stats stats{};
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // host-buffer calls: a second stream for the chunked head copy, one event per chunk, and
+    // events around the whole copy-in (ev_io[0..1]) and the read-back (ev_io[2..3])
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> chunk_ev;
+    cudaEvent_t ev_io[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_free = nullptr;  // marks earlier work on the stream before the chunked copies
+    bool have_io = false;
     cudaStream_t last_stream = nullptr;
     Control* ctl = nullptr;
     bool pending = false;      // a device call whose status has not been read yet
@@ -47,7 +56,8 @@ constexpr size_t ALIGN = 256;
 inline size_t align_up(size_t x) { return (x + ALIGN - 1) & ~(ALIGN - 1); }
 
 struct Layout {
-    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, vdesc = 0, headp = 0, ltiles = 0, thist = 0, spanning = 0,
+    size_t ctl = 0, deg = 0, dplus = 0, tile_i0 = 0, vdesc = 0, headp = 0, ltiles = 0, thist = 0, tkeys = 0,
+           spanning = 0,
            partials = 0, cnt = 0,
            total = 0, mid = 0, big = 0, scratch = 0, in_fo = 0, in_head = 0, bytes = 0;
     bool wide = false;
@@ -88,6 +98,7 @@ Layout make_layout(u64 n, u64 nnz, int32_t method, int num_sms, bool with_inputs
         // medium- and large-owner tiles, and both reordered
         L.ltiles = take(sizeof(uint2) * 4 * ktri::large_tile_capacity(n, nnz, small_d, seg));
         L.thist = take(sizeof(u32) * ktri::tile_order_scratch_words());
+        L.tkeys = take(sizeof(u32) * ktri::large_tile_capacity(n, nnz, small_d, seg));
         grid = (u32)(sms * 48);  // bound on the small + medium + large persistent grids (occupancy <= 16 each)
     } else {
         L.mid = take(sizeof(u32) * (n + 1));
@@ -139,7 +150,23 @@ ktri::Options resolve(const ktri_opts* o) {
     r.force_wide = o->force_wide_offsets != 0;
     if (o->medium_outdegree) r.medium_outdegree = o->medium_outdegree;
     if (o->segment) r.segment = o->segment;
+    r.copy_wait_polls = o->copy_wait_polls;
+    r.tile_order = o->tile_order;
     return r;
+}
+
+// Pieces of head copied at a time by the host-buffer entry points (graphs with at least two
+// pieces of adjacency are copied in pieces, overlapping the orientation).
+constexpr u64 HEAD_CHUNK_BYTES = u64(64) << 20;
+
+int ensure_chunk_events(ktri_ctx* ctx, size_t count) {
+    if (!ctx->copy_stream) KTRI_CK(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while (ctx->chunk_ev.size() < count) {
+        cudaEvent_t e = nullptr;
+        KTRI_CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->chunk_ev.push_back(e);
+    }
+    return KTRI_OK;
 }
 
 int ensure_ws(ktri_ctx* ctx, size_t bytes) {
@@ -183,10 +210,26 @@ struct DeviceGuard {
     }
 };
 
+// head arriving in pieces: chunk c holds adjacency slots [ends[c-1], ends[c]) and is on the
+// device once events[c] has completed.  Orientation tiles run as soon as their slots are in.
+struct HeadChunks {
+    int count = 0;
+    const u64* ends = nullptr;
+    const cudaEvent_t* events = nullptr;
+};
+
+// Polls of the large-owner kernel's first bulk-copy wait for an option value.
+u32 first_wait_polls(uint32_t opt) {
+    return opt == 0 ? ktri::COPY_WAIT_POLLS : (opt == KTRI_COPY_WAIT_NONE ? 0u : opt);
+}
+
+// The launch sequence of one count on the workspace at base.  ctx may be NULL (the
+// no-allocation entry point): errors then carry no message and no events are recorded.
 template <typename OffT>
-int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz,
-                     u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all, bool events,
-                     ktri::TriangleSink sink = ktri::TriangleSink{}) {
+int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const u64* fo, const u32* head, u64 n,
+                     u64 nnz, u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all,
+                     bool events, ktri::TriangleSink sink = ktri::TriangleSink{}, const HeadChunks* chunks = nullptr) {
+    events = events && ctx;
     auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
     auto* deg = reinterpret_cast<u32*>(base + L.deg);
     auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
@@ -195,18 +238,32 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     auto* spanning = reinterpret_cast<u32*>(base + L.spanning);
     auto* partials = reinterpret_cast<u64*>(base + L.partials);
     auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
-    const int sms = ctx->num_sms;
 
     KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
     const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
     ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
-    ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
+    if (!chunks) {
+        ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
+    } else {
+        // tile t reads slots below (t + 1) * ORIENT_TILE + 1: launch each tile once its slots are in
+        u64 done = 0;
+        for (int c = 0; c < chunks->count; ++c) {
+            KTRI_CK(ctx, cudaStreamWaitEvent(st, chunks->events[c], 0));
+            const u64 upto = c + 1 == chunks->count ? ktri::orient_tiles(n, nnz)
+                                                    : (chunks->ends[c] - 1) / ktri::ORIENT_TILE;
+            if (upto > done) {
+                ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st, done, upto);
+                done = upto;
+            }
+        }
+    }
     auto* mtiles = autom ? reinterpret_cast<uint2*>(base + L.ltiles) : nullptr;
     const u64 tcap = ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment);
     auto* ltiles = autom ? mtiles + tcap : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
-                            opt.medium_outdegree, opt.segment, ctl, sms, st);
+                            opt.medium_outdegree, opt.segment, opt.small_warp ? ktri::SMALL_WARP_DEG : 0xFFFFFFFFu,
+                            ctl, sms, st);
     // Tile orders (large tiles by the vertex range they stream, for L2 reuse; medium tiles
     // longest owner first, so the warps' last tiles are short).  Below 2^20 adjacency entries
     // everything fits L2 and the few tiles are not worth the four extra launches.
@@ -216,9 +273,13 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
     if (order) {
         lrun = ltiles + tcap;
         mrun = lrun + tcap;
-        ktri::launch_order_tiles(fo, head, dplus, n, ltiles, &ctl->large_tiles, opt.segment, false,
+        const bool by_cost = opt.tile_order == KTRI_TILE_ORDER_COST;
+        auto* keys = reinterpret_cast<u32*>(base + L.tkeys);
+        ktri::launch_order_tiles(fo, head, dplus, n, ltiles, &ctl->large_tiles, opt.segment,
+                                 by_cost ? ktri::TILE_BY_COST : ktri::TILE_BY_VERTEX, keys,
                                  reinterpret_cast<u32*>(base + L.thist), lrun, ctl, sms, st);
-        ktri::launch_order_tiles(fo, head, dplus, n, mtiles, &ctl->medium_tiles, opt.segment, true,
+        ktri::launch_order_tiles(fo, head, dplus, n, mtiles, &ctl->medium_tiles, opt.segment,
+                                 by_cost ? ktri::TILE_BY_COST : ktri::TILE_BY_DEGREE, keys,
                                  reinterpret_cast<u32*>(base + L.thist), mrun, ctl, sms, st);
     }
     if (!autom) {
@@ -227,15 +288,18 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
                                       L.scratch_per_block, L.big_grid, ctl, sms, st);
     }
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[1], st));
-    if (opt.collect_stats) ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, ctl, sms, st);
+    if (opt.collect_stats)
+        ktri::launch_stats<OffT>(fo, head, n, vdesc, headp, autom ? opt.medium_outdegree : 0xFFFFFFFFu, ctl, sms, st);
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
     if (sort_all) {
         // orientation export only: no counting
     } else if (autom) {
         KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mrun, lrun,
                                                    opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
-                                                   events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr));
-        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, opt.small_outdegree), d_total, ctl, st);
+                                                   events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr,
+                                                   first_wait_polls(opt.copy_wait_polls), opt.small_warp));
+        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, opt.small_outdegree, opt.small_warp),
+                           d_total, ctl, st);
     } else {
         const int grid = ktri::count_grid_edges(sms);
         ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
@@ -251,9 +315,10 @@ int enqueue_pipeline(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, 
 template <typename OffT>
 int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total,
                  u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all,
-                 ktri::TriangleSink sink = ktri::TriangleSink{}) {
+                 ktri::TriangleSink sink = ktri::TriangleSink{}, const HeadChunks* chunks = nullptr) {
     char* base = static_cast<char*>(ctx->ws);
-    const int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, sort_all, true, sink);
+    const int rc = enqueue_pipeline<OffT>(ctx, ctx->num_sms, base, L, fo, head, n, nnz, d_total, cnt, opt, st, sort_all,
+                                          true, sink, chunks);
     if (rc) return rc;
     ctx->ctl = reinterpret_cast<Control*>(base + L.ctl);
     ctx->last_stream = st;
@@ -261,6 +326,7 @@ int run_pipeline(ktri_ctx* ctx, const Layout& L, const u64* fo, const u32* head,
     ctx->have_events = true;
     ctx->last_method = opt.method;
     ctx->last_collect = opt.collect_stats;
+    ctx->have_io = false;
     ctx->stats = ktri_run_stats{};
     ctx->stats.n = n;
     ctx->stats.nnz = nnz;
@@ -302,6 +368,7 @@ int device_status(ktri_ctx* ctx) {
         ctx->stats.intersection_size_local = h.stat_isz;
         ctx->stats.streamed_entries = h.stat_streamed;
         ctx->stats.oriented_edges = h.stat_oriented;
+        ctx->stats.streamed_chunked = h.stat_chunked;
     }
     if (ctx->have_events) {
         float a = 0, b = 0, c = 0;
@@ -319,7 +386,20 @@ int device_status(ktri_ctx* ctx) {
             ctx->stats.ms_count_large = s2;
         }
     }
+    if (ctx->have_io) {
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, ctx->ev_io[0], ctx->ev_io[1]);
+        cudaEventElapsedTime(&b, ctx->ev_io[2], ctx->ev_io[3]);
+        cudaEventElapsedTime(&c, ctx->ev_io[0], ctx->ev_io[3]);
+        ctx->stats.ms_h2d = a;
+        ctx->stats.ms_d2h = b;
+        ctx->stats.ms_call = c;
+    }
     const u32 e = h.err & ktri::DEV_ERR_MASK;
+    if (e & ktri::DEV_ERR_COPY_INFLIGHT)
+        return set_error(ctx, KTRI_ERR_TIMEOUT, "a bulk copy into shared memory did not complete in time, not even "
+                                                "after a second wait: it may still have been in flight when its block "
+                                                "left, so treat the device state as suspect");
     if (e & ktri::DEV_ERR_TIMEOUT)
         return set_error(ctx, KTRI_ERR_TIMEOUT, "a bulk copy into shared memory did not complete in time");
     if (e & ktri::DEV_ERR_DEGREE)
@@ -340,54 +420,78 @@ std::map<int, ktri_ctx*> g_default;
 constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch, looked up once per device with that device current.
-// In host code the array's name is only a host-side stand-in, never a device address.
+// Device address of g_noalloc_scratch.  The array lives in this library's module, which the
+// CUDA runtime loads once per context, so the address is looked up (cudaGetSymbolAddress, with
+// the device current) once per device and context and cached under the context's unique id.
+// A new context on the same device (after cudaDeviceReset, or a driver-API caller that makes
+// its own context current) gets a fresh lookup instead of a stale address.
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+struct NoallocSlot {
+    unsigned long long ctx_id = 0;  // 0: no cached address
+    void* ptr = nullptr;
+};
+NoallocSlot g_noalloc_slot[NOALLOC_MAX_DEVICES];
+
+// Unique id of the calling thread's current CUDA context, through the driver entry points the
+// runtime hands out (no link against the driver library); 0 when it cannot be read.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 int noalloc_scratch(int device, void** out) {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES) return KTRI_ERR_NO_DEVICE;
+    const unsigned long long id = current_context_id();
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    NoallocSlot& slot = g_noalloc_slot[device];
+    if (id == 0 || slot.ctx_id != id || !slot.ptr) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
             return KTRI_ERR_CUDA;
         }
-        g_noalloc_ptr[device] = p;
+        slot.ptr = p;
+        // the lookup makes the device's context current if nothing had yet: key the address
+        // by the context it belongs to (0, never matched, when the id cannot be read)
+        slot.ctx_id = current_context_id();
     }
-    *out = g_noalloc_ptr[device];
+    *out = slot.ptr;
     return KTRI_OK;
 }
 
-// The AUTO pipeline (same kernels as ktri_count_csr_device) on a caller-free workspace.
+// The AUTO pipeline of ktri_count_csr_device (the same launch sequence, default options) on
+// the fixed scratch array.  enqueue_pipeline zeroes the control block; k_prep zeroes the
+// out-degrees and per-vertex counts; every other region is fully written before it is read.
 template <typename OffT>
 int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64 n, u64 nnz, u64* d_total, u64* cnt,
                 int sms, cudaStream_t st) {
-    auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
-    auto* deg = reinterpret_cast<u32*>(base + L.deg);
-    auto* dplus = reinterpret_cast<u32*>(base + L.dplus);
-    void* vdesc = base + L.vdesc;
-    auto* headp = reinterpret_cast<u32*>(base + L.headp);
-    auto* spanning = reinterpret_cast<u32*>(base + L.spanning);
-    auto* partials = reinterpret_cast<u64*>(base + L.partials);
-    auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
-    auto* mtiles = reinterpret_cast<uint2*>(base + L.ltiles);
-    auto* ltiles = mtiles + ktri::large_tile_capacity(n, nnz, (u32)ktri::SMALL_D_LOW, ktri::LARGE_SEG);
-    // the control block (counters, error word) must start at zero; k_prep zeroes the
-    // out-degrees and per-vertex counts; every other region is fully written before it is read
-    if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return KTRI_ERR_CUDA;
-    ktri::launch_prep(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl, sms, st);
-    ktri::launch_orient(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning, ctl, st);
-    ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, (u32)ktri::SMALL_D_LOW, (u32)ktri::MEDIUM_D,
-                            ktri::LARGE_SEG, ctl, sms, st);
-    if (ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mtiles, ltiles, (u32)ktri::SMALL_D_LOW,
-                                      ktri::LARGE_SEG, cnt, partials, ctl, sms, st, nullptr, nullptr) != cudaSuccess)
+    const ktri::Options opt;  // AUTO, default owner bins and segment (the layout is sized for them)
+    if (enqueue_pipeline<OffT>(nullptr, sms, base, L, fo, head, n, nnz, d_total, cnt, opt, st, false, false) !=
+        KTRI_OK)
         return KTRI_ERR_CUDA;
-    ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, (u32)ktri::SMALL_D_LOW), d_total, ctl, st);
-    if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
+    auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
     u32 herr = 0;
     if (cudaMemcpyAsync(&herr, &ctl->err, sizeof(u32), cudaMemcpyDeviceToHost, st) != cudaSuccess) return KTRI_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return KTRI_ERR_CUDA;
@@ -423,6 +527,8 @@ int ktri_ctx_create(int device, ktri_ctx** out) {
         return KTRI_ERR_CUDA;
     }
     for (auto& e : ctx->ev) cudaEventCreate(&e);
+    for (auto& e : ctx->ev_io) cudaEventCreate(&e);
+    cudaEventCreateWithFlags(&ctx->ev_free, cudaEventDisableTiming);
     *out = ctx;
     return KTRI_OK;
 }
@@ -435,8 +541,14 @@ int ktri_ctx_destroy(ktri_ctx* ctx) {
         DeviceGuard g(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         if (ctx->ws) cudaFree(ctx->ws);
+        if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
         for (auto& e : ctx->ev)
             if (e) cudaEventDestroy(e);
+        for (auto& e : ctx->ev_io)
+            if (e) cudaEventDestroy(e);
+        for (auto e : ctx->chunk_ev) cudaEventDestroy(e);
+        if (ctx->ev_free) cudaEventDestroy(ctx->ev_free);
+        if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
@@ -556,14 +668,48 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
     auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
     auto* d_total = reinterpret_cast<u64*>(base + L.total);
     cudaStream_t st = ctx->stream;
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[0], st));
     KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
-    if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz, cudaMemcpyHostToDevice, st));
-    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false)
-                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false);
+    // head in pieces on the copy stream; the orientation tiles of each piece start on the
+    // counting stream as soon as it has landed, so the copy hides the orientation
+    HeadChunks chunks;
+    std::vector<u64> ends;
+    const u64 head_bytes = sizeof(u32) * nnz;
+    if (head_bytes >= 2 * HEAD_CHUNK_BYTES) {
+        const u64 per = HEAD_CHUNK_BYTES / sizeof(u32);
+        for (u64 e = per; e < nnz; e += per) ends.push_back(e);
+        ends.push_back(nnz);
+        rc = ensure_chunk_events(ctx, ends.size());
+        if (rc) return rc;
+        // the copies overwrite the workspace's input region: they wait for earlier work on st
+        KTRI_CK(ctx, cudaEventRecord(ctx->ev_free, st));
+        KTRI_CK(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_free, 0));
+        u64 b = 0;
+        for (size_t c = 0; c < ends.size(); ++c) {
+            KTRI_CK(ctx, cudaMemcpyAsync(d_head + b, head + b, sizeof(u32) * (ends[c] - b), cudaMemcpyHostToDevice,
+                                         ctx->copy_stream));
+            KTRI_CK(ctx, cudaEventRecord(ctx->chunk_ev[c], ctx->copy_stream));
+            b = ends[c];
+        }
+        KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[1], ctx->copy_stream));
+        chunks.count = (int)ends.size();
+        chunks.ends = ends.data();
+        chunks.events = ctx->chunk_ev.data();
+    } else {
+        if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, head_bytes, cudaMemcpyHostToDevice, st));
+        KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[1], st));
+    }
+    rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false, {},
+                                    chunks.count ? &chunks : nullptr)
+                : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false, {},
+                                    chunks.count ? &chunks : nullptr);
     if (rc) return rc;
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[2], st));
     KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
     if (per_vertex_out)
         KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[3], st));
+    ctx->have_io = true;
     rc = device_status(ctx);
     if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
     return rc;
@@ -1002,7 +1148,8 @@ int enqueue_batch(ktri_ctx* ctx, char* base, const Layout& L, const u64* fo, con
                   const u64* graph_first, u64 num_graphs, u64* totals, u64* cnt, const ktri::Options& opt,
                   cudaStream_t st, bool events) {
     auto* d_total = reinterpret_cast<u64*>(base + L.total);
-    int rc = enqueue_pipeline<OffT>(ctx, base, L, fo, head, n, nnz, d_total, cnt, opt, st, false, events);
+    int rc = enqueue_pipeline<OffT>(ctx, ctx->num_sms, base, L, fo, head, n, nnz, d_total, cnt, opt, st, false,
+                                    events);
     if (rc) return rc;
     ktri::launch_graph_totals(cnt, graph_first, num_graphs, n, totals, reinterpret_cast<Control*>(base + L.ctl),
                               ctx->num_sms, st);
@@ -1150,8 +1297,10 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
     }
     // occupancy queries happen once, outside the capture
     for (u32 sd : {(u32)ktri::SMALL_D_LOW, (u32)ktri::SMALL_D}) {
-        (void)ktri::count_grid_auto<u32>(ctx->num_sms, sd);
-        (void)ktri::count_grid_auto<u64>(ctx->num_sms, sd);
+        for (bool w : {false, true}) {
+            (void)ktri::count_grid_auto<u32>(ctx->num_sms, sd, w);
+            (void)ktri::count_grid_auto<u64>(ctx->num_sms, sd, w);
+        }
     }
     cudaStream_t cs = nullptr;
     cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);

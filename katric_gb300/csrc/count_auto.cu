@@ -61,10 +61,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, u32 parit
         : "memory");
     return ok != 0;
 }
-// Waits for the barrier's phase of the given parity; gives up after a bounded number of polls
-// (each poll itself blocks for a short hardware-defined time) and reports false.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, u32 parity) {
-    for (u32 it = 0; it < (1u << 22); ++it)
+// Waits for the barrier's phase of the given parity; gives up after `polls` polls (each poll
+// itself blocks for a short hardware-defined time) and reports false.  polls = 0 gives up at
+// once without looking.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, u32 parity, u32 polls) {
+    for (u32 it = 0; it < polls; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -413,6 +414,123 @@ __global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict_
     if (threadIdx.x == 0) partials[blockIdx.x] = bt;
 }
 
+// Small owners, one warp per owner (the form used when Options.small_kernel selects it): a
+// warp takes 32 consecutive vertices at a time and, for each owner among them (out-degree
+// 1..small_outdegree, degree at most SMALL_WARP_DEG; owners of larger degree go to the medium
+// kernel's tiles), fills its own slice of shared memory with the owner's table and streams the
+// out-list of every lower neighbour through it, one list per lane.  No block barrier: the warps
+// of a block never wait for one another.
+template <int SD>
+struct SmallWarpLayout {
+    static constexpr int TS = SD <= 32 ? 64 : 128;  // table slots: a power of two >= 2 * SD
+    static constexpr int PER_WARP = TS + TS / 2;     // keys, then two 16-bit hit counters per word
+};
+
+template <int BLOCK, int SD, typename OffT>
+__global__ void __launch_bounds__(BLOCK, 4) k_count_small_warp(const u64* __restrict__ fo, const u32* __restrict__ head,
+                                                            u64 n, const Desc<OffT>* __restrict__ vdesc,
+                                                            const u32* __restrict__ headp, u32 sd,
+                                                            u64* __restrict__ cnt, u64* __restrict__ partials,
+                                                            Control* ctl) {
+    using L = SmallWarpLayout<SD>;
+    constexpr int NW = BLOCK / 32;
+    static_assert(2 * SD <= L::TS, "a table holds twice the owner's keys");
+    __shared__ __align__(16) u32 s_tab[NW * L::PER_WARP];
+    __shared__ u64 s_red[NW];
+    if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32* keys = s_tab + warp * L::PER_WARP;
+    u32* hitc = keys + L::TS;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    const u64 nbatch = (n + 31) / 32;
+    u64 local_total = 0;
+    u32 dup = 0;
+    while (true) {
+        unsigned long long bi = 0;
+        if (lane == 0) bi = atomicAdd(&ctl->small_next, 1ull);
+        bi = __shfl_sync(0xFFFFFFFFu, bi, 0);
+        if (bi >= nbatch) break;
+        const u64 v = bi * 32 + lane;
+        Desc<OffT> dv;
+        dv.start = 0;
+        dv.d = 0;
+        u64 a = 0, b = 0;
+        bool own = false;
+        if (v < n) {
+            dv = load_desc(vdesc + v);
+            a = fo[v];
+            b = fo[v + 1];
+            own = dv.d > 0 && dv.d <= sd && b - a <= (u64)SMALL_WARP_DEG;
+        }
+        const u64 vs = list_start(dv);
+        u32 todo = __ballot_sync(0xFFFFFFFFu, own);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const u64 x = bi * 32 + src;
+            const u32 dx = __shfl_sync(0xFFFFFFFFu, dv.d, src);
+            const u64 xs = __shfl_sync(0xFFFFFFFFu, vs, src);
+            const u64 xa = __shfl_sync(0xFFFFFFFFu, a, src);
+            const u32 xdeg = (u32)(__shfl_sync(0xFFFFFFFFu, b, src) - xa);
+            u32 lg = ceil_log2(2 * dx);
+            if (lg < 2) lg = 2;
+            const u32 size = 1u << lg;
+            for (u32 i = lane; i < size; i += 32) keys[i] = EMPTY_KEY;
+            for (u32 i = lane; i < size / 2; i += 32) hitc[i] = 0;
+            __syncwarp();
+            for (u32 q = lane; q < dx; q += 32)
+                if (!bucket_insert(keys, lg, __ldg(headp + xs + q))) dup = 1;
+            __syncwarp();
+            u32 T = 0;
+            for (u32 e0 = 0; e0 < xdeg; e0 += 32) {
+                u32 hits = 0;
+                if (e0 + lane < xdeg) {
+                    const u32 y = __ldg(head + xa + e0 + lane);
+                    if (y < n) {
+                        const Desc<OffT> vy = load_desc(vdesc + y);
+                        const u32 dy = vy.d;
+                        if (dy > 0 && key_less(dy, y, dx, x)) {
+                            // the list's 16-byte groups, four loads in flight before the probes
+                            const u64 q0 = list_group(vy);
+                            for (u32 g0 = 0; 4 * g0 < dy; g0 += 4) {
+                                uint4 qv[4];
+#pragma unroll
+                                for (int c = 0; c < 4; ++c)
+                                    qv[c] = 4 * (g0 + c) < dy ? __ldg(headp4 + q0 + g0 + c)
+                                                              : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+#pragma unroll
+                                for (int c = 0; c < 4; ++c) {
+                                    const u32 e = 4 * (g0 + c);
+                                    if (e < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
+                                    if (e + 1 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
+                                    if (e + 2 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
+                                    if (e + 3 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
+                                }
+                            }
+                            if (hits) atomicAdd(&cnt[y], (u64)hits);
+                        }
+                    }
+                }
+                T += hits;
+            }
+            __syncwarp();
+            for (u32 i = lane; i < size; i += 32) {
+                const u32 h = read16(hitc, i);
+                if (h) atomicAdd(&cnt[keys[i]], (u64)h);
+            }
+            T = __reduce_add_sync(0xFFFFFFFFu, T);
+            if (lane == 0 && T) {
+                atomicAdd(&cnt[x], (u64)T);
+                local_total += T;
+            }
+            __syncwarp();  // the next owner clears the table only after every lane has flushed
+        }
+    }
+    if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+    const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = bt;
+}
+
 template <int BLOCK, int CAP, typename OffT>
 struct LargeLayout {
     static constexpr int TS = 2 * CAP;       // table slots (at most half full)
@@ -520,7 +638,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                                                        const u32* __restrict__ headp,
                                                        const uint2* __restrict__ ltiles, u32 seg,
                                                        u64* __restrict__ cnt, u64* __restrict__ partials,
-                                                       Control* ctl) {
+                                                       Control* ctl, u32 first_wait_polls) {
     using L = LargeLayout<BLOCK, CAP, OffT>;
     constexpr int NW = BLOCK / 32;
     constexpr int U = 8;  // loads in flight per lane and list
@@ -541,7 +659,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
     fence_proxy_async_smem();
     __syncthreads();
     u32 phase = 0;
-    bool timed_out = false;
+    bool timed_out = false, inflight = false;
     // the owner's keys are staged in the queue's descriptor region, which is free until the scan
     u32* stage = reinterpret_cast<u32*>(smem + L::off_qd);
     static_assert(sizeof(Desc<OffT>) * LARGE_SEG >= sizeof(u32) * CAP, "staging fits the queue region");
@@ -586,12 +704,13 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                 mbar_expect_tx(&s_bar, bytes);
                 bulk_copy_g2s(stage, headp + list_start(dxd) + c0, bytes, &s_bar);
             }
-            const bool arrived = mbar_wait_bounded(&s_bar, phase);
+            const bool arrived = mbar_wait_bounded(&s_bar, phase, first_wait_polls);
             if (__syncthreads_or(!arrived)) {  // the same decision in every thread
                 // give the copy in flight a second bounded wait, so that it does not land in
-                // shared memory after the block has left; then report the timeout
-                (void)mbar_wait_bounded(&s_bar, phase);
-                timed_out = true;
+                // shared memory after the block has left; then report the timeout (and, if the
+                // copy still has not landed, that it may be in flight as the block leaves)
+                if (!__syncthreads_or(!mbar_wait_bounded(&s_bar, phase, COPY_WAIT_POLLS))) timed_out = true;
+                else timed_out = inflight = true;
                 break;
             }
             phase ^= 1u;
@@ -671,7 +790,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         if (timed_out) break;
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
-    if (timed_out) atomicOr(&ctl->err, DEV_ERR_TIMEOUT);
+    if (timed_out) atomicOr(&ctl->err, DEV_ERR_TIMEOUT | (inflight ? DEV_ERR_COPY_INFLIGHT : 0u));
     if (threadIdx.x == 0) partials[blockIdx.x] = local_total;
 }
 
@@ -791,9 +910,16 @@ __global__ void __launch_bounds__(BLOCK)
     if (threadIdx.x == 0) partials[blockIdx.x] = bt;
 }
 
-// Sum of the per-block partial totals (a u64 tree reduction in one block).
-__global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials, u32 np, u64* total) {
+// Sum of the per-block partial totals (a u64 tree reduction in one block).  After a device
+// error (invalid input, a bounded wait that ran out) the partials are incomplete or stale, so
+// the total is written as 0.
+__global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials, u32 np, u64* total,
+                                                const Control* ctl) {
     __shared__ u64 s_red[32];
+    if (*(volatile const u32*)&ctl->err & DEV_ERR_MASK) {
+        if (threadIdx.x == 0) *total = 0;
+        return;
+    }
     u64 s = 0;
     for (u32 i = threadIdx.x; i < np; i += 1024) s += partials[i];
     const u64 t = block_sum_u64<1024>(s, s_red);
@@ -822,17 +948,21 @@ __global__ void __launch_bounds__(256) k_graph_totals(const u64* __restrict__ cn
 }
 
 // collect_stats: wedge_checks = sum over oriented (v,u) of |N+(u)|, the reference's counter
-// (cetric_edge_iterator.h:279-281), plus the entries streamed by the AUTO kernels.
+// (cetric_edge_iterator.h:279-281), plus the entries streamed by the AUTO kernels, also counted
+// once per table chunk of their owner (owners above medium_d keep at most LARGE_CAP keys per
+// chunk and stream their segment once per chunk).
 template <typename OffT>
 __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
-                        const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp, Control* ctl) {
+                        const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp, u32 medium_d,
+                        Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
     const u64 gw = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
-    u64 wedge = 0, isz = 0, streamed = 0, oriented = 0;
+    u64 wedge = 0, isz = 0, streamed = 0, oriented = 0, chunked = 0;
     for (u64 v = gw; v < n; v += nwarps) {
         const Desc<OffT> dv = load_desc(vdesc + v);
+        const u64 chunks = dv.d > medium_d ? (dv.d + LARGE_CAP - 1) / LARGE_CAP : 1;
         if (lane == 0) oriented += dv.d;
         for (u32 k = lane; k < dv.d; k += 32) {
             const u32 u = headp[list_start(dv) + k];
@@ -843,7 +973,10 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
         for (u64 e = fo[v] + lane; e < fo[v + 1]; e += 32) {
             const u32 y = head[e];
             const u32 dy = load_desc(vdesc + y).d;
-            if (dy > 0 && key_less(dy, y, dv.d, v)) streamed += dy;
+            if (dy > 0 && key_less(dy, y, dv.d, v)) {
+                streamed += dy;
+                chunked += dy * chunks;
+            }
         }
     }
 #pragma unroll
@@ -852,12 +985,14 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
         isz += __shfl_down_sync(0xFFFFFFFFu, isz, o);
         streamed += __shfl_down_sync(0xFFFFFFFFu, streamed, o);
         oriented += __shfl_down_sync(0xFFFFFFFFu, oriented, o);
+        chunked += __shfl_down_sync(0xFFFFFFFFu, chunked, o);
     }
     if (lane == 0) {
         atomicAdd(&ctl->stat_wedge, wedge);
         atomicAdd(&ctl->stat_isz, isz);
         atomicAdd(&ctl->stat_streamed, streamed);
         atomicAdd(&ctl->stat_oriented, oriented);
+        atomicAdd(&ctl->stat_chunked, chunked);
     }
 }
 
@@ -878,6 +1013,16 @@ int occupancy_small() {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<SD, OffT>::bytes);
         int o = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<SD, OffT>::bytes);
+        occ = o > 0 ? o : 1;
+    }
+    return occ;
+}
+template <int SD, typename OffT>
+int occupancy_small_warp() {
+    static int occ = -1;
+    if (occ < 0) {
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_count_small_warp<SMALL_BLOCK, SD, OffT>, SMALL_BLOCK, 0);
         occ = o > 0 ? o : 1;
     }
     return occ;
@@ -909,7 +1054,10 @@ int occupancy_large() {
 }  // namespace
 
 template <typename OffT>
-int count_grid_small(int num_sms, u32 small_d) {
+int count_grid_small(int num_sms, u32 small_d, bool warp) {
+    if (warp)
+        return num_sms * (small_d <= (u32)SMALL_D_LOW ? occupancy_small_warp<SMALL_D_LOW, OffT>()
+                                                      : occupancy_small_warp<SMALL_D, OffT>());
     return num_sms * (small_d <= (u32)SMALL_D_LOW ? occupancy_small<SMALL_D_LOW, OffT>()
                                                   : occupancy_small<SMALL_D, OffT>());
 }
@@ -922,8 +1070,8 @@ int count_grid_large(int num_sms) {
     return num_sms * occupancy_large<OffT>();
 }
 template <typename OffT>
-int count_grid_auto(int num_sms, u32 small_d) {
-    return count_grid_small<OffT>(num_sms, small_d) + count_grid_medium<OffT>(num_sms) +
+int count_grid_auto(int num_sms, u32 small_d, bool warp) {
+    return count_grid_small<OffT>(num_sms, small_d, warp) + count_grid_medium<OffT>(num_sms) +
            count_grid_large<OffT>(num_sms);
 }
 
@@ -931,12 +1079,19 @@ template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
                               const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
                               u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
-                              cudaEvent_t after_small, cudaEvent_t after_large) {
-    const int gs = count_grid_small<OffT>(num_sms, small_d);
+                              cudaEvent_t after_small, cudaEvent_t after_large, u32 copy_wait_polls,
+                              bool small_warp) {
+    const int gs = count_grid_small<OffT>(num_sms, small_d, small_warp);
     const int gm = count_grid_medium<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
-    if (small_d <= (u32)SMALL_D_LOW)
+    if (small_warp && small_d <= (u32)SMALL_D_LOW)
+        k_count_small_warp<SMALL_BLOCK, SMALL_D_LOW, OffT>
+            <<<gs, SMALL_BLOCK, 0, st>>>(fo, head, n, vd, headp, small_d, cnt, partials, ctl);
+    else if (small_warp)
+        k_count_small_warp<SMALL_BLOCK, SMALL_D, OffT>
+            <<<gs, SMALL_BLOCK, 0, st>>>(fo, head, n, vd, headp, small_d, cnt, partials, ctl);
+    else if (small_d <= (u32)SMALL_D_LOW)
         k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D_LOW, OffT><<<gs, SMALL_BLOCK, SmallL<SMALL_D_LOW, OffT>::bytes, st>>>(
             fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials, ctl);
     else
@@ -947,7 +1102,7 @@ cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, co
         <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, seg, cnt, partials + gs, ctl);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
         <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, seg, cnt, partials + gs + gm,
-                                                       ctl);
+                                                       ctl, copy_wait_polls);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
 }
@@ -960,32 +1115,36 @@ void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs,
 }
 
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st) {
-    (void)ctl;
-    k_final<<<1, 1024, 0, st>>>(partials, np, total);
+    k_final<<<1, 1024, 0, st>>>(partials, np, total, ctl);
 }
 
 template <typename OffT>
-void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
-                  int num_sms, cudaStream_t st) {
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, u32 medium_d,
+                  Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
-    k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp, ctl);
+    k_stats<OffT><<<num_sms * 8, 256, 0, st>>>(fo, head, n, reinterpret_cast<const Desc<OffT>*>(vdesc), headp,
+                                               medium_d, ctl);
 }
 
-template int count_grid_small<u32>(int, u32);
-template int count_grid_small<u64>(int, u32);
+template int count_grid_small<u32>(int, u32, bool);
+template int count_grid_small<u64>(int, u32, bool);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
 template int count_grid_medium<u32>(int);
 template int count_grid_medium<u64>(int);
-template int count_grid_auto<u32>(int, u32);
-template int count_grid_auto<u64>(int, u32);
+template int count_grid_auto<u32>(int, u32, bool);
+template int count_grid_auto<u64>(int, u32, bool);
 template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
                                             const uint2*, const uint2*, u32, u32,
-                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
+                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t, u32,
+                                            bool);
 template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
                                             const uint2*, const uint2*, u32, u32,
-                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t);
-template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
-template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, Control*, int, cudaStream_t);
+                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t, u32,
+                                            bool);
+template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, u32, Control*, int,
+                                cudaStream_t);
+template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, u32, Control*, int,
+                                cudaStream_t);
 
 }  // namespace ktri

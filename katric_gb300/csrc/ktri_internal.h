@@ -25,6 +25,9 @@ struct Options {
     uint64_t binary_cutoff = 1000;
     double hybrid_scale = 1.0;
     bool force_wide = false;
+    uint32_t copy_wait_polls = 0;    // polls of the first wait for an owner chunk's bulk copy (0 = default)
+    uint32_t tile_order = 0;         // 0: by streamed vertex / owner degree; KTRI_TILE_ORDER_COST: by tile work
+    bool small_warp = false;         // small owners: warp-per-owner kernel instead of merge-path tiles
 };
 
 // The device a context was created on.
@@ -37,6 +40,8 @@ enum : uint32_t {
     DEV_ERR_DUPLICATE = 1u << 2,  // a list holds the same id twice
     DEV_ERR_DEGREE = 1u << 3,     // first_out not monotone, or a degree >= 2^32
     DEV_ERR_TIMEOUT = 1u << 4,    // a bounded wait (bulk-copy barrier) ran out
+    DEV_ERR_COPY_INFLIGHT = 1u << 5,  // ... and its second wait too: a copy may have been in flight
+                                      // into shared memory when the block left
     DEV_FLAG_UNSORTED = 1u << 8,  // some input list is not strictly increasing (not an error)
 };
 
@@ -57,7 +62,8 @@ struct Control {
     unsigned long long sort_big;         // lists sorted by whole blocks in global scratch
     unsigned long long medium_tiles;     // number of (owner, segment) tiles for medium owners
     unsigned long long medium_next;      // dynamic tile cursor of the medium-owner kernel
-    unsigned long long pad[2];
+    unsigned long long stat_chunked;     // collect_stats: streamed entries times the owner's table chunks
+    unsigned long long pad[1];
 };
 
 }  // namespace ktri

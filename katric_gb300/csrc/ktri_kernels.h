@@ -26,6 +26,9 @@ constexpr int LARGE_CAP = 2048;      // keys per shared-memory table chunk of th
 constexpr u32 LARGE_SEG = 1024;      // most adjacency slots per (owner, segment) tile
 constexpr u32 MIN_SEG = 64;          // fewest adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
+constexpr u32 COPY_WAIT_POLLS = 1u << 22;  // polls of a bounded wait for a bulk copy into shared memory
+constexpr u32 SMALL_WARP_DEG = 256;  // the warp-per-owner small kernel takes owners up to this degree; owners
+                                     // of larger degree (and small out-degree) go to the medium kernel's tiles
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
 // Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
@@ -35,10 +38,10 @@ constexpr u64 TILE_BASE = (u64)SMALL_BLOCK * SMALL_IPT;
 constexpr u64 ORIENT_PER_BASE = (u64)ORIENT_BLOCK * ORIENT_IPT / TILE_BASE;
 static_assert(ORIENT_PER_BASE * TILE_BASE == (u64)ORIENT_BLOCK * ORIENT_IPT, "orientation tile = whole base tiles");
 inline u64 base_tiles(u64 n, u64 nnz) { return (n + nnz + TILE_BASE - 1) / TILE_BASE; }
-// Owners above small_d hold more than small_d adjacency entries each; every owner has at most
-// deg / seg + 1 tiles.
+// Owners above small_d hold more than small_d adjacency entries each, and owners routed to the
+// tiles for their degree more than SMALL_WARP_DEG; every owner has at most deg / seg + 1 tiles.
 inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d, u32 seg) {
-    u64 owners = nnz / ((u64)small_d + 1) + 1;
+    u64 owners = nnz / ((u64)small_d + 1) + nnz / ((u64)SMALL_WARP_DEG + 1) + 1;
     if (owners > n) owners = n;
     return owners + nnz / seg + 1;
 }
@@ -75,36 +78,49 @@ struct TriangleSink {
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
                  int num_sms, cudaStream_t st);
+// Orientation over merge-path tiles [tile_begin, tile_end) of ORIENT_TILE items (all by
+// default).  Tile t reads adjacency slots below (t + 1) * ORIENT_TILE + 1 only, so it may run
+// as soon as that prefix of head is on the device.
+constexpr u64 ORIENT_TILE = (u64)ORIENT_BLOCK * ORIENT_IPT;
+u64 orient_tiles(u64 n, u64 nnz);
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
-                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st);
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st, u64 tile_begin = 0,
+                   u64 tile_end = ~0ull);
 // Owner tiles: medium owners' tiles are written to mtiles, large owners' to ltiles (each
 // array holds large_tile_capacity entries).
+// small_deg_max: owners up to small_d whose degree exceeds it get medium tiles too (the
+// warp-per-owner small kernel's bound; ~0u with the tile kernel, which takes any degree).
 template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
-                 u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st);
+                 u32 medium_d, u32 seg, u32 small_deg_max, Control* ctl, int num_sms, cudaStream_t st);
 
-// Owner tiles reordered (*count tiles on the device): by the first vertex their segment streams,
-// or with by_degree by their owner's out-degree, largest first.  hist needs
+// Owner tiles reordered (*count tiles on the device) by a counting sort on a 12-bit key:
+// TILE_BY_VERTEX, the first vertex each segment streams (tiles that run together then stream
+// from the same region of the list array); TILE_BY_DEGREE, the owner's out-degree, largest
+// first; TILE_BY_COST, the tile's streamed entries (k_tile_cost writes them, log-scaled, into
+// keys, which needs the tiles' capacity in u32), heaviest first.  hist needs
 // tile_order_scratch_words() u32, sorted the same capacity as tiles.
+enum : u32 { TILE_BY_VERTEX = 0, TILE_BY_DEGREE = 1, TILE_BY_COST = 2 };
 u64 tile_order_scratch_words();
 void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n, const uint2* tiles,
-                        const unsigned long long* count, u32 seg, bool by_degree, u32* hist, uint2* sorted,
+                        const unsigned long long* count, u32 seg, u32 mode, u32* keys, u32* hist, uint2* sorted,
                         Control* ctl, int num_sms, cudaStream_t st);
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
-int count_grid_small(int num_sms, u32 small_d);
+int count_grid_small(int num_sms, u32 small_d, bool warp);
 template <typename OffT>
 int count_grid_medium(int num_sms);
 template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
-int count_grid_auto(int num_sms, u32 small_d);  // small + medium + large, for this small-owner bound
+int count_grid_auto(int num_sms, u32 small_d, bool warp);  // small + medium + large, for this small-owner bound
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
                               const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
                               u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
-                              cudaEvent_t after_small, cudaEvent_t after_large);
+                              cudaEvent_t after_small, cudaEvent_t after_large,
+                              u32 copy_wait_polls = COPY_WAIT_POLLS, bool small_warp = false);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
 
 // u64 ids (the binary file format) -> u32 ids; ids above 2^32 - 1 become 0xFFFFFFFF.
@@ -133,8 +149,8 @@ void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs,
 // Work counters of the reference (wedge_checks, intersection_size_local) and of the AUTO
 // kernels, accumulated into the control block.
 template <typename OffT>
-void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, Control* ctl,
-                  int num_sms, cudaStream_t st);
+void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, const u32* headp, u32 medium_d,
+                  Control* ctl, int num_sms, cudaStream_t st);
 
 // Sorted-list strategies (merge, binary search, binary, hybrid): sort out-lists by id, then
 // one warp per oriented edge.

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
                                                   u64 nnz, const u32* __restrict__ deg,
                                                   const u32* __restrict__ tile_i0, u32* __restrict__ headp,
                                                   u32* __restrict__ dplus, u32* __restrict__ spanning,
-                                                  Control* ctl) {
+                                                  Control* ctl, u64 tile_begin) {
     constexpr int TILE = BLOCK * IPT;
     // Everything inside a tile is addressed relative to its first vertex i0 and first slot j0,
     // in 32 bits.  s_fo[k] = first_out[i0 + k] - j0 clamped to [0, nslot]: only the first
@@ -66,13 +66,14 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
 
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 total = n + nnz;
-    const u64 d0 = (u64)blockIdx.x * TILE;
+    const u64 tile = tile_begin + blockIdx.x;
+    const u64 d0 = tile * TILE;
     if (d0 >= total) return;
     const u64 d1 = d0 + TILE < total ? d0 + TILE : total;
     if (threadIdx.x == 0) {
         const u64 nt = (total + TILE_BASE - 1) / TILE_BASE;
-        const u64 k1 = ORIENT_PER_BASE * ((u64)blockIdx.x + 1);
-        s_b[0] = tile_i0[ORIENT_PER_BASE * (u64)blockIdx.x];
+        const u64 k1 = ORIENT_PER_BASE * (tile + 1);
+        s_b[0] = tile_i0[ORIENT_PER_BASE * tile];
         s_b[1] = tile_i0[k1 < nt ? k1 : nt];
     }
     __syncthreads();
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
 template <typename OffT>
 __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict__ dplus, Desc<OffT>* __restrict__ vdesc,
                        uint2* __restrict__ mtiles, uint2* __restrict__ ltiles, u32 small_d, u32 medium_d, u32 seg,
-                       Control* ctl) {
+                       u32 small_deg_max, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31;
     const u64 warp_global = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -254,7 +255,8 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
             ds.d = d;
             if constexpr (sizeof(OffT) == 8) ds.pad = 0;
             vdesc[v] = ds;
-            const u32 nt = d > small_d ? (u32)((b - a + seg - 1) / seg) : 0u;
+            const bool tiled = d > small_d || (d > 0 && b - a > small_deg_max);
+            const u32 nt = tiled ? (u32)((b - a + seg - 1) / seg) : 0u;
             if (d > medium_d) nl = nt;
             else nm = nt;
         }
@@ -285,12 +287,15 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
 // serves the repeats.  Counts do not depend on the order.
 constexpr u32 TILE_BUCKETS = 4096;
 
-// Sort key of a tile: the top id bits of the first vertex its segment streams (by_degree =
-// false), or the owner's out-degree, largest first (by_degree = true: longest tiles first).
+// Sort key of a tile (TILE_BY_VERTEX): the top id bits of the first vertex its segment
+// streams; (TILE_BY_DEGREE): the owner's out-degree, largest first (longest tiles first);
+// (TILE_BY_COST): the key k_tile_cost left in keys[t].
 __device__ __forceinline__ u32 tile_key(const u64* fo, const u32* head, const u32* dplus, uint2 tl, u32 seg,
-                                        u32 shift, bool by_degree) {
+                                        u32 shift, u32 mode, const u32* keys, u64 t) {
     u32 key;
-    if (by_degree) {
+    if (mode == TILE_BY_COST) {
+        key = keys[t];
+    } else if (mode == TILE_BY_DEGREE) {
         const u32 d = dplus[tl.x];
         key = d >= TILE_BUCKETS ? 0u : TILE_BUCKETS - 1 - d;
     } else {
@@ -299,14 +304,49 @@ __device__ __forceinline__ u32 tile_key(const u64* fo, const u32* head, const u3
     return key < TILE_BUCKETS ? key : TILE_BUCKETS - 1;
 }
 
+// The work of each tile, for TILE_BY_COST: the entries its owner x streams over the tile's
+// segment, sum of d+(y) over the neighbours y below x in (out-degree, id) -- the edge cost of
+// the reference's DPD cost function (cost_function.h:287-376, cetric_edge_iterator.h:584-593)
+// restated for owner-side tiles.  One warp per tile; the key orders heaviest first on a
+// log scale (7 fractional bits).
+__global__ void k_tile_cost(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
+                            const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg,
+                            u32* __restrict__ keys, Control* ctl) {
+    if (ctl->err & DEV_ERR_MASK) return;
+    const u64 nt = *(volatile const unsigned long long*)count;
+    const int lane = threadIdx.x & 31;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 t = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+        const uint2 tl = tiles[t];
+        const u64 x = tl.x;
+        const u32 dx = dplus[x];
+        const u64 a = fo[x] + (u64)tl.y * seg, e1 = fo[x + 1], b = a + seg < e1 ? a + seg : e1;
+        u64 cost = 0;
+        for (u64 e = a + lane; e < b; e += 32) {
+            const u32 y = __ldg(head + e);
+            const u32 dy = __ldg(dplus + y);
+            if (dy > 0 && key_less(dy, y, dx, x)) cost += dy;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cost += __shfl_down_sync(0xFFFFFFFFu, cost, o);
+        if (lane == 0) {
+            const u32 c = cost > 0xFFFFFFFFull ? 0xFFFFFFFFu : (u32)cost;
+            const u32 lg = 31 - __clz(c | 1u);
+            const u32 frac = lg >= 7 ? (c >> (lg - 7)) & 0x7Fu : (c << (7 - lg)) & 0x7Fu;
+            const u32 bucket = lg * 128 + frac;  // < 32 * 128 = TILE_BUCKETS
+            keys[t] = TILE_BUCKETS - 1 - bucket;
+        }
+    }
+}
+
 __global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
                             const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
-                            bool by_degree, u32* hist, Control* ctl) {
+                            u32 mode, const u32* __restrict__ keys, u32* hist, Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride)
-        atomicAdd(&hist[tile_key(fo, head, dplus, tiles[t], seg, shift, by_degree)], 1u);
+        atomicAdd(&hist[tile_key(fo, head, dplus, tiles[t], seg, shift, mode, keys, t)], 1u);
 }
 
 __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
@@ -330,13 +370,14 @@ __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
 
 __global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
                                const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
-                               bool by_degree, u32* cursor, uint2* __restrict__ sorted, Control* ctl) {
+                               u32 mode, const u32* __restrict__ keys, u32* cursor, uint2* __restrict__ sorted,
+                               Control* ctl) {
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
     const u64 stride = (u64)gridDim.x * blockDim.x;
     for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
         const uint2 tl = tiles[t];
-        sorted[atomicAdd(&cursor[tile_key(fo, head, dplus, tl, seg, shift, by_degree)], 1u)] = tl;
+        sorted[atomicAdd(&cursor[tile_key(fo, head, dplus, tl, seg, shift, mode, keys, t)], 1u)] = tl;
     }
 }
 
@@ -345,16 +386,18 @@ __global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict
 u64 tile_order_scratch_words() { return TILE_BUCKETS; }
 
 void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n, const uint2* tiles,
-                        const unsigned long long* count, u32 seg, bool by_degree, u32* hist, uint2* sorted,
+                        const unsigned long long* count, u32 seg, u32 mode, u32* keys, u32* hist, uint2* sorted,
                         Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u32 bits = 0;
     while ((1ull << bits) < n) ++bits;
     const u32 shift = bits > 12 ? bits - 12 : 0;
     cudaMemsetAsync(hist, 0, sizeof(u32) * TILE_BUCKETS, st);
-    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, by_degree, hist, ctl);
+    if (mode == TILE_BY_COST)
+        k_tile_cost<<<num_sms * 8, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, keys, ctl);
+    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, ctl);
     k_tile_scan<<<1, 1024, 0, st>>>(hist, ctl);
-    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, by_degree, hist, sorted,
+    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, sorted,
                                                 ctl);
 }
 
@@ -366,29 +409,32 @@ void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, 
     k_prep<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(fo, n, nnz, deg, dplus, cnt, tile_i0, ctl);
 }
 
+u64 orient_tiles(u64 n, u64 nnz) { return (n + nnz + ORIENT_TILE - 1) / ORIENT_TILE; }
+
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
-                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st) {
+                   u32* dplus, u32* spanning, Control* ctl, cudaStream_t st, u64 tile_begin, u64 tile_end) {
     constexpr int BLOCK = ORIENT_BLOCK, IPT = ORIENT_IPT;
-    const u64 total = n + nnz;
-    if (total == 0) return;
-    const u64 tiles = (total + BLOCK * IPT - 1) / (BLOCK * IPT);
-    k_orient<BLOCK, IPT><<<(unsigned)tiles, BLOCK, 0, st>>>(fo, head, n, nnz, deg, tile_i0, headp, dplus, spanning,
-                                                             ctl);
+    const u64 tiles = orient_tiles(n, nnz);
+    if (tile_end > tiles) tile_end = tiles;
+    if (tile_begin >= tile_end) return;
+    k_orient<BLOCK, IPT><<<(unsigned)(tile_end - tile_begin), BLOCK, 0, st>>>(fo, head, n, nnz, deg, tile_i0, headp,
+                                                                             dplus, spanning, ctl, tile_begin);
 }
 
 template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
-                 u32 medium_d, u32 seg, Control* ctl, int num_sms, cudaStream_t st) {
+                 u32 medium_d, u32 seg, u32 small_deg_max, Control* ctl, int num_sms, cudaStream_t st) {
     if (n == 0) return;
     u64 blocks = (n + 255) / 256;
     u64 cap = (u64)num_sms * 8;
     k_desc<OffT><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(
-        fo, n, dplus, reinterpret_cast<Desc<OffT>*>(vdesc), mtiles, ltiles, small_d, medium_d, seg, ctl);
+        fo, n, dplus, reinterpret_cast<Desc<OffT>*>(vdesc), mtiles, ltiles, small_d, medium_d, seg, small_deg_max,
+        ctl);
 }
 
-template void launch_desc<u32>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, Control*, int,
-                               cudaStream_t);
-template void launch_desc<u64>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, Control*, int,
-                               cudaStream_t);
+template void launch_desc<u32>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, u32, Control*,
+                               int, cudaStream_t);
+template void launch_desc<u64>(const u64*, u64, const u32*, void*, uint2*, uint2*, u32, u32, u32, u32, Control*,
+                               int, cudaStream_t);
 
 }  // namespace ktri

@@ -7,8 +7,9 @@
 // Search: the library default (KTRI_METHOD_AUTO with bins 32 / 256, segment 1024) is timed
 // first; then the reference's strategies (hybrid first; merge, binary search and binary only
 // when hybrid comes within 1.5x of the best); then, if an AUTO configuration is best, one pass
-// of coordinate descent over small_outdegree, medium_outdegree and segment.  A candidate
-// replaces the best configuration so far only when it is more than 2 % faster.
+// of coordinate descent over small_outdegree, medium_outdegree and segment, and last the tile
+// order by streamed work (KTRI_TILE_ORDER_COST).  A candidate replaces the best configuration so
+// far only when it is more than 2 % faster.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,9 +53,9 @@ int floor_log2(u64 x) {
 
 struct Cand {
     int32_t method = KTRI_METHOD_AUTO;
-    uint32_t small = 32, medium = 256, seg = 1024;
+    uint32_t small = 32, medium = 256, seg = 1024, order = 0;
     bool operator==(const Cand& o) const {
-        return method == o.method && small == o.small && medium == o.medium && seg == o.seg;
+        return method == o.method && small == o.small && medium == o.medium && seg == o.seg && order == o.order;
     }
 };
 
@@ -74,14 +75,16 @@ bool read_cache(const char* path, const std::string& sig, Cand* c, double* ms) {
     };
     while (std::getline(f, line)) {
         if (line.find(key) == std::string::npos) continue;
-        double m, s, md, sg, t;
+        double m, s, md, sg, t, to = 0;
         if (!field(line, "method", &m) || !field(line, "small_outdegree", &s) ||
             !field(line, "medium_outdegree", &md) || !field(line, "segment", &sg) || !field(line, "ms", &t))
             continue;
+        field(line, "tile_order", &to);  // absent in lines written before the option existed
         c->method = (int32_t)m;
         c->small = (uint32_t)s;
         c->medium = (uint32_t)md;
         c->seg = (uint32_t)sg;
+        c->order = (uint32_t)to;
         *ms = t;
         found = true;
     }
@@ -94,8 +97,9 @@ bool append_cache(const char* path, const std::string& sig, const Cand& c, doubl
     if (!f) return false;
     std::fprintf(f,
                  "{\"signature\": \"%s\", \"method\": %d, \"small_outdegree\": %u, \"medium_outdegree\": %u, "
-                 "\"segment\": %u, \"ms\": %.6f, \"default_ms\": %.6f, \"candidates\": %u, \"version\": \"%s\"}\n",
-                 sig.c_str(), c.method, c.small, c.medium, c.seg, ms, default_ms, candidates, ktri_version());
+                 "\"segment\": %u, \"tile_order\": %u, \"ms\": %.6f, \"default_ms\": %.6f, \"candidates\": %u, "
+                 "\"version\": \"%s\"}\n",
+                 sig.c_str(), c.method, c.small, c.medium, c.seg, c.order, ms, default_ms, candidates, ktri_version());
     return std::fclose(f) == 0;
 }
 
@@ -178,6 +182,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                 o.small_outdegree = c.small;
                 o.medium_outdegree = c.medium;
                 o.segment = c.seg;
+                o.tile_order = c.order;
                 double bestt = 1e30;
                 for (int rep = 0; rep < 4; ++rep) {
                     cudaEventRecord(e0, st);
@@ -264,6 +269,16 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
                     }
                 }
                 if (rc) break;
+                // the tiles taken heaviest first by their streamed work (the reference's DPD
+                // edge cost per tile) instead of by locality
+                Cand c = best;
+                c.order = KTRI_TILE_ORDER_COST;
+                rc = timed(c, &t);
+                if (rc) break;
+                if (clearly_faster(t, best_ms)) {
+                    best = c;
+                    best_ms = t;
+                }
             }
             res.ms = best_ms;
             if (cache_path && !append_cache(cache_path, sig, best, best_ms, res.default_ms, res.candidates)) {
@@ -275,6 +290,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
         res.small_outdegree = best.small;
         res.medium_outdegree = best.medium;
         res.segment = best.seg;
+        res.tile_order = best.order;
     } while (false);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
@@ -291,6 +307,7 @@ extern "C" int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const u
         o.small_outdegree = res.small_outdegree;
         o.medium_outdegree = res.medium_outdegree;
         o.segment = res.segment;
+        o.tile_order = res.tile_order;
         std::memcpy(opts, &o, std::min<size_t>(keep, sizeof(ktri_opts)));
         opts->struct_size = keep;
         *out = res;

@@ -386,27 +386,50 @@ int orc_max_threads(void) {
 #endif
 }
 
-/* CPU-baseline helper: preprocessing of the whole graph, then the node-parallel local phase
- * restricted to a deterministic 1/sample_stride subset of tail vertices (v is kept when a
- * hash of v is divisible by sample_stride).  Used to time a bounded, unbiased sample of a
- * large workload: the local-phase time of the whole graph is estimated as the sample's
- * time times sample_stride.  Returns the triangles whose lowest vertex is in the sample. */
-uint64_t orc_run_shmem_sampled(uint64_t n, const uint64_t* fo, uint32_t* work_head, int method, uint64_t cutoff,
-                               double hybrid_scale, int num_threads, uint64_t sample_stride, orc_stats* st) {
-    uint64_t* offset = (uint64_t*)malloc((n ? n : 1) * sizeof(uint64_t));
-    orc_stats local;
-    memset(&local, 0, sizeof local);
-    orc_preprocess(n, fo, work_head, offset, num_threads, &local);
+/* Slice of a vertex set by a hash of the id: vertex v belongs to slice hash(v) mod slices. */
+static inline uint64_t slice_of(uint32_t v, uint64_t slices) {
+    uint64_t h = (uint64_t)v * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    return h % slices;
+}
+
+/* One timed piece of a full run_shmem count, for the CPU baseline: the vertices of one hash
+ * slice have their lists copied back from the input, oriented and id-sorted (the per-vertex
+ * work of preprocessing, shared_memory_cetric.h:72-103), then the node-parallel local phase
+ * (cetric_edge_iterator.h:889-1066, merge or the configured strategy) runs over the same
+ * vertices as tails.  work_head/offset must hold a fully preprocessed graph (orc_preprocess)
+ * so that the out-lists of the other slices are in place; re-orienting a slice reproduces the
+ * same lists.  Running the slices 0..slices-1 once each does the work of exactly one count.
+ * Returns the triangles whose tail vertex is in the slice; *adj_out receives the slice's
+ * degree sum (twice its share of the undirected edges; the slices' sums add up to nnz). */
+uint64_t orc_count_slice(uint64_t n, const uint64_t* fo, const uint32_t* head, uint32_t* work_head, uint64_t* offset,
+                         uint64_t slice, uint64_t slices, int method, int num_threads, uint64_t* adj_out,
+                         orc_stats* st) {
+    if (slices == 0) slices = 1;
     double t0 = now_s();
-    uint64_t tri = 0, wedges = 0, isz = 0, sampled = 0;
-    if (sample_stride == 0) sample_stride = 1;
-#pragma omp parallel for schedule(dynamic, 64) num_threads(num_threads) reduction(+ : tri, wedges, isz, sampled)
+    uint64_t deg2 = 0;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(num_threads) reduction(+ : deg2)
     for (int64_t vi = 0; vi < (int64_t)n; ++vi) {
         uint32_t v = (uint32_t)vi;
-        uint64_t h = (uint64_t)v * 0x9E3779B97F4A7C15ull;
-        h ^= h >> 29;
-        if (h % sample_stride) continue;
-        sampled++;
+        if (slice_of(v, slices) != slice) continue;
+        uint64_t b = fo[v], e = fo[v + 1];
+        memcpy(work_head + b, head + b, (e - b) * sizeof(uint32_t));
+        offset[v] = orient_vertex(work_head, fo, v);
+        deg2 += e - b;
+    }
+    double t1 = now_s();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(num_threads)
+    for (int64_t vi = 0; vi < (int64_t)n; ++vi) {
+        uint32_t v = (uint32_t)vi;
+        if (slice_of(v, slices) != slice) continue;
+        sort_vertex(work_head, fo, offset, v);
+    }
+    double t2 = now_s();
+    uint64_t tri = 0, wedges = 0, isz = 0;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(num_threads) reduction(+ : tri, wedges, isz)
+    for (int64_t vi = 0; vi < (int64_t)n; ++vi) {
+        uint32_t v = (uint32_t)vi;
+        if (slice_of(v, slices) != slice) continue;
         const uint32_t* nv = work_head + fo[v] + offset[v];
         uint64_t dv = fo[v + 1] - fo[v] - offset[v];
         for (uint64_t k = 0; k < dv; ++k) {
@@ -415,18 +438,22 @@ uint64_t orc_run_shmem_sampled(uint64_t n, const uint64_t* fo, uint32_t* work_he
             uint64_t du = fo[u + 1] - fo[u] - offset[u];
             wedges += du;
             isz += dv + du;
-            emit_t e;
-            memset(&e, 0, sizeof e);
-            intersect(nv, dv, nu, du, method, cutoff, hybrid_scale, &e);
-            tri += e.hits;
+            emit_t em;
+            memset(&em, 0, sizeof em);
+            intersect(nv, dv, nu, du, method, 1000, 1.0, &em);
+            tri += em.hits;
         }
     }
-    local.local_phase_s = now_s() - t0;
-    local.triangles = tri;
-    local.wedge_checks = wedges;
-    local.intersection_size_local = isz;
-    local.skipped_nodes = n - sampled;
-    free(offset);
-    if (st) *st = local;
+    double t3 = now_s();
+    if (adj_out) *adj_out = deg2;
+    if (st) {
+        memset(st, 0, sizeof *st);
+        st->triangles = tri;
+        st->wedge_checks = wedges;
+        st->intersection_size_local = isz;
+        st->orientation_s = t1 - t0;
+        st->sorting_s = t2 - t1;
+        st->local_phase_s = t3 - t2;
+    }
     return tri;
 }

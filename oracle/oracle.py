@@ -58,9 +58,11 @@ def lib() -> ctypes.CDLL:
                                     ctypes.POINTER(OrcStats)]
         L.orc_oriented_csr.restype = U64
         L.orc_oriented_csr.argtypes = [U64, P, P, P, P]
-        L.orc_run_shmem_sampled.restype = U64
-        L.orc_run_shmem_sampled.argtypes = [U64, P, P, ctypes.c_int, U64, ctypes.c_double, ctypes.c_int, U64,
-                                            ctypes.POINTER(OrcStats)]
+        L.orc_preprocess.restype = None
+        L.orc_preprocess.argtypes = [U64, P, P, P, ctypes.c_int, ctypes.POINTER(OrcStats)]
+        L.orc_count_slice.restype = U64
+        L.orc_count_slice.argtypes = [U64, P, P, P, P, U64, U64, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(U64), ctypes.POINTER(OrcStats)]
         L.orc_max_threads.restype = ctypes.c_int
         L.orc_max_threads.argtypes = []
         _lib = L
@@ -96,15 +98,34 @@ def count(first_out, head, method: str = "merge", num_threads: int = 1, per_vert
     return int(total), (pv[:n] if pv is not None else None), stats
 
 
-def count_sampled(first_out, head, sample_stride: int, method: str = "merge", num_threads: int = 1):
-    """Whole-graph preprocessing, then the local phase over a 1/sample_stride sample of tail
-    vertices.  Returns (triangles in the sample, stats dict with the phase times)."""
-    fo = np.ascontiguousarray(first_out, dtype=np.uint64)
-    work = np.array(head, dtype=np.uint32, copy=True)
-    st = OrcStats()
-    t = lib().orc_run_shmem_sampled(len(fo) - 1, _ptr(fo), _ptr(work), METHODS[method], 1000, 1.0,
-                                    int(num_threads), int(sample_stride), ctypes.byref(st))
-    return int(t), {k: getattr(st, k) for k, _ in OrcStats._fields_}
+class SlicedCount:
+    """A full run_shmem count cut into pieces for timing: vertex v belongs to slice
+    hash(v) mod slices; piece s orients and id-sorts the lists of slice s (copied back from the
+    input) and runs the node-parallel local phase over slice s's tail vertices.  Pieces
+    0..slices-1 together do exactly the work of one count, and their triangles add up to the
+    total.  Construction preprocesses the whole graph once (outside any timing), so each piece
+    finds the other slices' out-lists in place."""
+
+    def __init__(self, first_out, head, slices: int, method: str = "merge", num_threads: int = 1):
+        self.fo = np.ascontiguousarray(first_out, dtype=np.uint64)
+        self.head = np.ascontiguousarray(head, dtype=np.uint32)
+        self.n = len(self.fo) - 1
+        self.work = np.array(self.head, dtype=np.uint32, copy=True)
+        self.offset = np.zeros(max(self.n, 1), dtype=np.uint64)
+        self.slices = int(slices)
+        self.method = METHODS[method]
+        self.threads = int(num_threads)
+        lib().orc_preprocess(self.n, _ptr(self.fo), _ptr(self.work), _ptr(self.offset), self.threads, None)
+
+    def run(self, s: int):
+        """Piece s: returns (triangles with their tail in slice s, adjacency entries of slice s,
+        stats dict with the piece's orientation, sorting and local-phase seconds)."""
+        st = OrcStats()
+        adj = ctypes.c_uint64(0)
+        t = lib().orc_count_slice(self.n, _ptr(self.fo), _ptr(self.head), _ptr(self.work), _ptr(self.offset),
+                                  int(s) % self.slices, self.slices, self.method, self.threads, ctypes.byref(adj),
+                                  ctypes.byref(st))
+        return int(t), int(adj.value), {k: getattr(st, k) for k, _ in OrcStats._fields_}
 
 
 def oriented_csr(first_out, head):

@@ -1,5 +1,7 @@
 """The device-resident entry point (ktri_count_csr_device) on torch-allocated buffers and
 streams, and size-independent properties at large sizes (needs a GB300)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -75,3 +77,19 @@ def test_memory_budget(counter):
         assert e.value.code == _native.ERR_OUT_OF_MEMORY
         small.set_memory_budget(0)
         assert small.count(g.first_out, g.head)[0] == counter.count(g.first_out, g.head)[0]
+
+
+def test_host_path_copies_head_in_pieces(counter, oracle):
+    """Host buffers of more than two 64 MiB pieces of adjacency: head is copied in pieces on a
+    second stream and the orientation tiles of each piece start as soon as it lands.  Counts
+    must equal the oracle's, and the call reports its copy / read-back split."""
+    g = Graph.rmat(21, 16, seed=5)
+    assert 4 * g.nnz >= 2 * (64 << 20)
+    total, pv, _ = oracle.count(g.first_out, g.head, num_threads=os.cpu_count() or 4)
+    for _ in range(2):
+        t, p = counter.count(g.first_out, g.head, Config())
+        assert t == total and np.array_equal(p, pv)
+        st = counter.stats()
+        assert 0 < st.ms_h2d <= st.ms_call and 0 < st.ms_d2h <= st.ms_call
+    t, p = counter.count(g.first_out, g.head, Config(intersection_method="merge"))
+    assert t == total and np.array_equal(p, pv)

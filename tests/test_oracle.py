@@ -151,5 +151,7 @@ def test_work_counters_match_their_definition(oracle):
     for method in METHODS:
         t, _, st = oracle.count(fo, head, method=method, num_threads=2)
         assert st["wedge_checks"] == wedges and st["intersection_size_local"] == isz, method
-        ts, sst = oracle.count_sampled(fo, head, 1, method=method, num_threads=2)
-        assert ts == t and sst["wedge_checks"] == wedges, method
+        sc = oracle.SlicedCount(fo, head, 3, method=method, num_threads=2)
+        parts = [sc.run(s) for s in range(3)]
+        assert sum(p[0] for p in parts) == t and sum(p[1] for p in parts) == len(head), method
+        assert sum(p[2]["wedge_checks"] for p in parts) == wedges, method

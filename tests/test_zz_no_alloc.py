@@ -59,6 +59,29 @@ def test_noalloc_matches_device_entry_point(kind):
         assert np.array_equal(out.cpu().numpy().view(np.uint64), pv)
 
 
+def test_noalloc_near_the_limit_against_the_oracle(oracle):
+    """RMAT scale 18 (7.6e6 adjacency entries, a 45 MiB workspace): big enough that the tile
+    orders run, with owners above out-degree 256 (the large-owner kernel and its bulk copies),
+    checked against the CPU oracle, twice in a row."""
+    torch = pytest.importorskip("torch")
+    g = Graph.rmat(18, 16, seed=2)
+    L = _native.load()
+    ws = L.ktri_workspace_bytes(g.n, g.nnz, _native.METHOD_AUTO)
+    assert SCRATCH_BYTES // 2 < ws <= SCRATCH_BYTES and g.nnz >= 1 << 20
+    ofo, _ = oracle.oriented_csr(g.first_out, g.head)
+    assert int(np.diff(ofo).max()) > 256  # some owner runs in the large-owner kernel
+    total, pv, _ = oracle.count(g.first_out, g.head, num_threads=8)
+    fo, hd = _dev(g.first_out, torch), _dev(g.head, torch)
+    for _ in range(2):
+        tot = torch.full((1,), -1, dtype=torch.int64, device="cuda")
+        out = torch.full((g.n,), -1, dtype=torch.int64, device="cuda")
+        rc = L.ktri_count_csr_device_noalloc(fo.data_ptr(), hd.data_ptr(), g.n, g.nnz, tot.data_ptr(),
+                                             out.data_ptr(), None)
+        assert rc == _native.OK
+        assert int(tot.item()) == total
+        assert np.array_equal(out.cpu().numpy().view(np.uint64), pv)
+
+
 def test_noalloc_refuses_graphs_beyond_the_scratch():
     torch = pytest.importorskip("torch")
     L = _native.load()
