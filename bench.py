@@ -392,6 +392,7 @@ def run_batch(args, steps: int, warmup: int, plain_passes: int = 3) -> dict:
         plain.append((time.perf_counter() - t1) * 1e3)
     plain_ms = statistics.median(plain)
     del per, fo, hd, pv
+    plan.close()
     ctr.close()
     return {
         "workload": name, "graphs": k, "n_total": n, "m_total": b.union.m, "seed": w["seed"],

@@ -183,7 +183,8 @@ int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_
  * replayed by ktri_plan_launch (one graph launch instead of one launch per kernel).  The plan
  * owns its workspace and is bound to the device buffers given here; refill those buffers with
  * another batch of the same n_total / nnz_total / num_graphs and launch again.
- * ktri_plan_check synchronises the last launch and reports invalid input found on the device. */
+ * ktri_plan_check synchronises the last launch and reports invalid input found on the device.
+ * Launch and check need the plan's context alive; destroy does not. */
 typedef struct ktri_plan ktri_plan;
 int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
                            uint64_t nnz_total, const uint64_t* d_graph_first, uint64_t num_graphs,

@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes
 import dataclasses
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -111,10 +112,13 @@ class TriangleCounter:
         _native.check(self._L.ktri_ctx_create(device, ctypes.byref(h)))
         self._ctx = h
         self.device = device
+        self._plans = weakref.WeakSet()  # plans bound to this context, closed before it
         if memory_budget:
             self.set_memory_budget(memory_budget)
 
     def close(self) -> None:
+        for plan in list(getattr(self, "_plans", ())):
+            plan.close()
         if getattr(self, "_ctx", None) is not None:
             self._L.ktri_ctx_destroy(self._ctx)
             self._ctx = None
@@ -291,7 +295,9 @@ class TriangleCounter:
         self._check(self._L.ktri_plan_create_batch(self._ctx, first_out_ptr, head_ptr, n_total, nnz_total,
                                                    graph_first_ptr, num_graphs, totals_ptr, per_vertex_ptr,
                                                    ctypes.byref(opts), ctypes.byref(h)))
-        return Plan(self, h)
+        plan = Plan(self, h)
+        self._plans.add(plan)
+        return plan
 
     def autotune(self, first_out_ptr: int, head_ptr: int, n: int, nnz: int, graph_first_ptr: int | None = None,
                  num_graphs: int = 0, cache_path: str | None = None, conf: Config | None = None,

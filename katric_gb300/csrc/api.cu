@@ -239,6 +239,9 @@ int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const 
     auto* partials = reinterpret_cast<u64*>(base + L.partials);
     auto* tile_i0 = reinterpret_cast<u32*>(base + L.tile_i0);
 
+    // an error a caller's own failed runtime call left in this thread must not be taken for a
+    // failed launch of ours below (errors of kernels that faulted are sticky and stay visible)
+    (void)cudaGetLastError();
     KTRI_CK(ctx, cudaMemsetAsync(ctl, 0, sizeof(Control), st));
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[0], st));
     const bool autom = opt.method == KTRI_METHOD_AUTO && !sort_all;
@@ -1260,7 +1263,8 @@ int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_
 }  // extern "C"
 
 struct ktri_plan {
-    ktri_ctx* ctx = nullptr;
+    ktri_ctx* ctx = nullptr;  // launch and check report errors through it
+    int device = 0;           // destroy needs only this, so it is safe after the context is gone
     void* ws = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1289,6 +1293,7 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
     ktri_plan* p = new (std::nothrow) ktri_plan();
     if (!p) return KTRI_ERR_OUT_OF_MEMORY;
     p->ctx = ctx;
+    p->device = ctx->device;
     cudaError_t e = cudaMalloc(&p->ws, L.bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1366,7 +1371,7 @@ int ktri_plan_check(ktri_plan* plan) {
 int ktri_plan_destroy(ktri_plan* plan) {
     if (!plan) return KTRI_ERR_INVALID_ARGUMENT;
     {
-        DeviceGuard g(plan->ctx->device);
+        DeviceGuard g(plan->device);
         if (plan->launched) cudaStreamSynchronize(plan->last);
         if (plan->exec) cudaGraphExecDestroy(plan->exec);
         if (plan->graph) cudaGraphDestroy(plan->graph);

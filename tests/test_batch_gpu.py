@@ -140,3 +140,39 @@ def test_autotune_persists_and_plans_exactly(counter, oracle, tmp_path):
     assert info3["candidates"] >= 5
     t, p = counter.count(g.first_out, g.head, conf3)
     assert t == oracle.count(g.first_out, g.head, num_threads=4)[0]
+
+
+def test_plan_destroyed_after_its_context():
+    """A plan may be destroyed after the context it was made on (a garbage-collected plan in a
+    host language can outlive an explicitly closed context): destroy touches only the plan, and
+    leaves no error behind for the next call on another context."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from katric_gb300 import Batch, Config, TriangleCounter, _native
+    L = _native.load()
+    b = Batch.generate(8, 6.0, 9.0, 4.0, 16.0, seed=11)
+    fo = torch.from_numpy(b.union.first_out.view(np.int64)).cuda()
+    hd = torch.from_numpy(b.union.head.view(np.int32)).cuda()
+    gf = torch.from_numpy(b.graph_first.view(np.int64)).cuda()
+    tot = torch.zeros(b.num_graphs, dtype=torch.int64, device="cuda")
+    ctx = ctypes.c_void_p()
+    assert L.ktri_ctx_create(0, ctypes.byref(ctx)) == _native.OK
+    plan = ctypes.c_void_p()
+    opts = Config().opts()
+    assert L.ktri_plan_create_batch(ctx, fo.data_ptr(), hd.data_ptr(), b.union.n, b.union.nnz, gf.data_ptr(),
+                                    b.num_graphs, tot.data_ptr(), None, ctypes.byref(opts),
+                                    ctypes.byref(plan)) == _native.OK
+    assert L.ktri_plan_launch(plan, None) == _native.OK
+    assert L.ktri_plan_check(plan) == _native.OK
+    expect = tot.clone()
+    assert L.ktri_ctx_destroy(ctx) == _native.OK
+    assert L.ktri_plan_destroy(plan) == _native.OK
+    with TriangleCounter(0) as ctr:
+        out = torch.zeros_like(tot)
+        ctr.count_batch_device(fo.data_ptr(), hd.data_ptr(), b.union.n, b.union.nnz, gf.data_ptr(), b.num_graphs,
+                               out.data_ptr(), None, Config())
+        ctr.check()
+        assert torch.equal(out, expect)
