@@ -649,7 +649,7 @@ def main():
         e2e_step()
     e2e_steps = max(3, min(args.steps, 10))
     barrier()
-    split = {"h2d": [], "d2h": [], "call": [], "orient": [], "count": []}
+    split = {"h2d": [], "d2h": [], "call": [], "orient": [], "count": [], "host_enqueue": [], "host_call": []}
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
@@ -659,6 +659,8 @@ def main():
         split["call"].append(st.ms_call)
         split["orient"].append(st.ms_orient)
         split["count"].append(st.ms_count)
+        split["host_enqueue"].append(st.host_ms_enqueue)
+        split["host_call"].append(st.host_ms_call)
     t1 = time.perf_counter()
     barrier()
     e2e_ms = (t1 - t0) * 1e3 / e2e_steps
@@ -706,7 +708,8 @@ def main():
                 "split_note": "device time inside ktri_count_csr_ctx (library events): h2d = first input copy to "
                               "last piece of head landed (orientation runs on the pieces already in), orient = "
                               "orientation phase incl. waiting for pieces, count = intersection phase, d2h = "
-                              "read-back of total + per-vertex counts, call = all of it"},
+                              "read-back of total + per-vertex counts, call = all of it; host_enqueue / host_call = host time "
+                              "until everything was enqueued / of the whole call"},
         "gpu_launches": kernels_per_count(g.nnz) * args.steps,
         "clocks": clk,
     }

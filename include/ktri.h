@@ -99,6 +99,9 @@ typedef struct ktri_run_stats {
                                          last piece of head has landed (orientation overlaps it) */
     float ms_d2h;                     /* host-buffer calls: device time of the read-back of the results */
     float ms_call;                    /* host-buffer calls: device time of the whole call, copies included */
+    float host_ms_enqueue;            /* host-buffer calls: host time from entry until every copy and launch
+                                         was enqueued (includes waiting where a copy to pageable memory blocks) */
+    float host_ms_call;               /* host-buffer calls: host time of the whole call */
     uint64_t streamed_chunked;        /* entries the AUTO kernels stream, counted once per owner-table chunk
                                          that streams them (collect_stats); above streamed_entries only when
                                          some owner has more than 2048 out-neighbours */

@@ -112,6 +112,8 @@ class RunStats(ctypes.Structure):
         ("ms_h2d", ctypes.c_float),
         ("ms_d2h", ctypes.c_float),
         ("ms_call", ctypes.c_float),
+        ("host_ms_enqueue", ctypes.c_float),
+        ("host_ms_call", ctypes.c_float),
         ("streamed_chunked", ctypes.c_uint64),
     ]
 

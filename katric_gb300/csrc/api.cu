@@ -6,6 +6,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -265,8 +266,8 @@ int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const 
     const u64 tcap = ktri::large_tile_capacity(n, nnz, opt.small_outdegree, opt.segment);
     auto* ltiles = autom ? mtiles + tcap : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
-                            opt.medium_outdegree, opt.segment, opt.small_warp ? ktri::SMALL_WARP_DEG : 0xFFFFFFFFu,
-                            ctl, sms, st);
+                            opt.medium_outdegree, opt.segment,
+                            autom && opt.small_warp ? ktri::SMALL_WARP_DEG : 0xFFFFFFFFu, ctl, sms, st);
     // Tile orders (large tiles by the vertex range they stream, for L2 reuse; medium tiles
     // longest owner first, so the warps' last tiles are short).  Below 2^20 adjacency entries
     // everything fits L2 and the few tiles are not worth the four extra launches.
@@ -650,6 +651,7 @@ int ktri_count_csr_device_noalloc(const uint64_t* d_first_out, const uint32_t* d
 
 int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz,
                        uint64_t* total_out, uint64_t* per_vertex_out, const ktri_opts* opts) {
+    const auto t_entry = std::chrono::steady_clock::now();
     const ktri::Options opt = resolve(opts);
     int rc = check_common(ctx, first_out, head, n, nnz, total_out, opt);
     if (rc) return rc;
@@ -713,8 +715,12 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
         KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
     KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[3], st));
     ctx->have_io = true;
+    const auto t_enqueued = std::chrono::steady_clock::now();
     rc = device_status(ctx);
     if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
+    const auto t_done = std::chrono::steady_clock::now();
+    ctx->stats.host_ms_enqueue = std::chrono::duration<float, std::milli>(t_enqueued - t_entry).count();
+    ctx->stats.host_ms_call = std::chrono::duration<float, std::milli>(t_done - t_entry).count();
     return rc;
 }
 

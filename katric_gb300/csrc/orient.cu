@@ -255,7 +255,8 @@ __global__ void k_desc(const u64* __restrict__ fo, u64 n, const u32* __restrict_
             ds.d = d;
             if constexpr (sizeof(OffT) == 8) ds.pad = 0;
             vdesc[v] = ds;
-            const bool tiled = d > small_d || (d > 0 && b - a > small_deg_max);
+            // no tiles at all without tile arrays (the reference strategies pass none)
+            const bool tiled = mtiles && ltiles && (d > small_d || (d > 0 && b - a > small_deg_max));
             const u32 nt = tiled ? (u32)((b - a + seg - 1) / seg) : 0u;
             if (d > medium_d) nl = nt;
             else nm = nt;

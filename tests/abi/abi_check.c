@@ -48,6 +48,8 @@ static int sizes(void) {
     FIELD(ktri_run_stats, ms_h2d);
     FIELD(ktri_run_stats, ms_d2h);
     FIELD(ktri_run_stats, ms_call);
+    FIELD(ktri_run_stats, host_ms_enqueue);
+    FIELD(ktri_run_stats, host_ms_call);
     FIELD(ktri_run_stats, streamed_chunked);
     printf("ktri_server_opts %zu\n", sizeof(ktri_server_opts));
     FIELD(ktri_server_opts, struct_size);
