@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import statistics
@@ -645,14 +646,18 @@ def main():
         if rc:
             raise katric_gb300.KtriError(rc, L.ktri_last_error(ctr.handle).decode())
 
-    for _ in range(2):
+    for _ in range(3):
         e2e_step()
     e2e_steps = max(3, min(args.steps, 10))
     barrier()
     split = {"h2d": [], "d2h": [], "call": [], "orient": [], "count": [], "host_enqueue": [], "host_call": []}
+    walls = []
+    gc.disable()  # no collector pause inside the timed region
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
         e2e_step()
+        walls.append((time.perf_counter() - ts) * 1e3)
         st = ctr.stats()  # device-side split of the call (the library's events)
         split["h2d"].append(st.ms_h2d)
         split["d2h"].append(st.ms_d2h)
@@ -662,6 +667,7 @@ def main():
         split["host_enqueue"].append(st.host_ms_enqueue)
         split["host_call"].append(st.host_ms_call)
     t1 = time.perf_counter()
+    gc.enable()
     barrier()
     e2e_ms = (t1 - t0) * 1e3 / e2e_steps
     assert tot.value == total_ref
@@ -704,6 +710,9 @@ def main():
                                        "dram__bytes_write.sum of the three counting kernels, one capture)"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8),
+                "call_wall_ms": {"min": min(walls), "median": statistics.median(walls), "max": max(walls),
+                                 "each": [round(x, 2) for x in walls],
+                                 "host_call_each": [round(x, 2) for x in split["host_call"]]},
                 "split_ms": {k: statistics.median(v) for k, v in split.items()},
                 "split_note": "device time inside ktri_count_csr_ctx (library events): h2d = first input copy to "
                               "last piece of head landed (orientation runs on the pieces already in), orient = "

@@ -313,7 +313,11 @@ typedef struct ktri_server_opts {
                                     memory; 0 (default): batches go through pinned host staging.  Direct access
                                     lowers latency at low load, but the driver may migrate the touched pages to
                                     the GPU, which slows the callers' later host accesses */
-    uint32_t reserved[6];
+    uint32_t engine;             /* 1: one persistent counting kernel (the engine) runs across batches; each batch
+                                    is prepared on its slot (orientation, owner tiles) and published to the
+                                    running engine as a job, so arrivals fold into the kernel that is already
+                                    counting.  0 (default): one counting launch sequence per batch */
+    uint32_t reserved[5];
 } ktri_server_opts;
 typedef struct ktri_server_stats {
     uint64_t submitted, completed, batches, batched_graphs, cache_hits, evictions, resident_graphs, resident_bytes,
@@ -323,7 +327,9 @@ typedef struct ktri_server_stats {
     uint64_t alloc_us;   /* of pack_us: time spent growing the slots' device and pinned host buffers */
     uint64_t harvest_us; /* worker time spent reading back results and keeping graphs resident */
     uint64_t device_us;  /* device time of the batches (first copy to last read-back), summed */
-    uint64_t reserved[2];
+    uint64_t engine_launches; /* launches of the persistent counting kernel (engine mode): it leaves when idle
+                                 and is launched again by the next published batch */
+    uint64_t reserved[1];
 } ktri_server_stats;
 int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** out);
 int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first_out, const uint32_t* head,

@@ -66,7 +66,8 @@ class ServerOpts(ctypes.Structure):
         ("max_batch_nnz", ctypes.c_uint64),
         ("max_batch_graphs", ctypes.c_uint32),
         ("direct_host_access", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 6),
+        ("engine", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 5),
     ]
 
 
@@ -74,7 +75,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "batches", "batched_graphs", "cache_hits",
                                               "evictions", "resident_graphs", "resident_bytes",
                                               "peak_inflight_batches", "coalesced", "pack_us", "alloc_us",
-                                              "harvest_us", "device_us")] + [("reserved", ctypes.c_uint64 * 2)]
+                                              "harvest_us", "device_us", "engine_launches")] + \
+        [("reserved", ctypes.c_uint64 * 1)]
 
 
 class Tuning(ctypes.Structure):

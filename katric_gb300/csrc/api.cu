@@ -219,6 +219,13 @@ struct HeadChunks {
     const cudaEvent_t* events = nullptr;
 };
 
+// Where a prepared batch goes instead of the counting kernels: an engine job slot.
+struct EnginePublish {
+    ktri::EngineJob* job = nullptr;
+    unsigned long long seq = 0;
+    unsigned long long* done_word = nullptr;  // device address of the host-mapped completion word
+};
+
 // Polls of the large-owner kernel's first bulk-copy wait for an option value.
 u32 first_wait_polls(uint32_t opt) {
     return opt == 0 ? ktri::COPY_WAIT_POLLS : (opt == KTRI_COPY_WAIT_NONE ? 0u : opt);
@@ -229,7 +236,8 @@ u32 first_wait_polls(uint32_t opt) {
 template <typename OffT>
 int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const u64* fo, const u32* head, u64 n,
                      u64 nnz, u64* d_total, u64* cnt, const ktri::Options& opt, cudaStream_t st, bool sort_all,
-                     bool events, ktri::TriangleSink sink = ktri::TriangleSink{}, const HeadChunks* chunks = nullptr) {
+                     bool events, ktri::TriangleSink sink = ktri::TriangleSink{}, const HeadChunks* chunks = nullptr,
+                     const EnginePublish* publish = nullptr) {
     events = events && ctx;
     auto* ctl = reinterpret_cast<Control*>(base + L.ctl);
     auto* deg = reinterpret_cast<u32*>(base + L.deg);
@@ -267,7 +275,7 @@ int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const 
     auto* ltiles = autom ? mtiles + tcap : nullptr;
     ktri::launch_desc<OffT>(fo, n, dplus, vdesc, mtiles, ltiles, autom ? opt.small_outdegree : 0xFFFFFFFFu,
                             opt.medium_outdegree, opt.segment,
-                            autom && opt.small_warp ? ktri::SMALL_WARP_DEG : 0xFFFFFFFFu, ctl, sms, st);
+                            autom ? ktri::SMALL_WARP_DEG : 0xFFFFFFFFu, ctl, sms, st);
     // Tile orders (large tiles by the vertex range they stream, for L2 reuse; medium tiles
     // longest owner first, so the warps' last tiles are short).  Below 2^20 adjacency entries
     // everything fits L2 and the few tiles are not worth the four extra launches.
@@ -297,13 +305,16 @@ int enqueue_pipeline(ktri_ctx* ctx, int sms, char* base, const Layout& L, const 
     if (events) KTRI_CK(ctx, cudaEventRecord(ctx->ev[2], st));
     if (sort_all) {
         // orientation export only: no counting
+    } else if (autom && publish) {
+        // the counting phase runs in the serving engine: publish the prepared batch as a job
+        ktri::launch_publish(publish->job, publish->seq, fo, head, n, vdesc, headp, mrun, lrun, cnt, ctl,
+                             opt.small_outdegree, opt.segment, publish->done_word, st);
     } else if (autom) {
-        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, tile_i0, mrun, lrun,
-                                                   opt.small_outdegree, opt.segment, cnt, partials, ctl, sms, st,
+        KTRI_CK(ctx, ktri::launch_count_auto<OffT>(fo, head, n, nnz, vdesc, headp, mrun, lrun, opt.small_outdegree,
+                                                   opt.segment, cnt, partials, ctl, sms, st,
                                                    events ? ctx->ev[4] : nullptr, events ? ctx->ev[5] : nullptr,
-                                                   first_wait_polls(opt.copy_wait_polls), opt.small_warp));
-        ktri::launch_final(partials, (u32)ktri::count_grid_auto<OffT>(sms, opt.small_outdegree, opt.small_warp),
-                           d_total, ctl, st);
+                                                   first_wait_polls(opt.copy_wait_polls)));
+        ktri::launch_final_auto<OffT>(partials, n, opt.small_outdegree, sms, d_total, ctl, st);
     } else {
         const int grid = ktri::count_grid_edges(sms);
         ktri::launch_count_edges<OffT>(n, vdesc, headp, opt.method, opt.binary_cutoff, opt.hybrid_scale, cnt, partials,
@@ -506,6 +517,46 @@ int run_noalloc(char* base, const Layout& L, const u64* fo, const u32* head, u64
 }  // namespace
 
 int ktri::ctx_device(const ktri_ctx* ctx) { return ctx->device; }
+
+int ktri::ctx_num_sms(const ktri_ctx* ctx) { return ctx->num_sms; }
+
+int ktri::engine_prepare_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                               uint64_t nnz_total, uint64_t* d_per_vertex, void* stream, ktri::EngineJob* job,
+                               unsigned long long seq, unsigned long long* done_word, ktri::Control** ctl_out) {
+    ktri::Options opt;  // AUTO with the default bins and segment
+    int rc = check_common(ctx, d_first_out, d_head, n_total, nnz_total, d_per_vertex, opt);
+    if (rc) return rc;
+    if (!d_per_vertex || !job || !done_word || n_total == 0) return KTRI_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(ctx->device);
+    if (ctx->pending) device_status(ctx);
+    const Layout L = make_layout(n_total, nnz_total, opt.method, ctx->num_sms, false, false, false,
+                                 opt.small_outdegree, opt.segment);
+    if (L.wide) return KTRI_ERR_UNSUPPORTED;  // the engine's jobs use 32-bit descriptors
+    rc = ensure_ws(ctx, L.bytes);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    char* base = static_cast<char*>(ctx->ws);
+    EnginePublish pub;
+    pub.job = job;
+    pub.seq = seq;
+    pub.done_word = done_word;
+    rc = enqueue_pipeline<u32>(ctx, ctx->num_sms, base, L, reinterpret_cast<const u64*>(d_first_out), d_head, n_total,
+                               nnz_total, reinterpret_cast<u64*>(base + L.total), reinterpret_cast<u64*>(d_per_vertex),
+                               opt, st, false, false, ktri::TriangleSink{}, nullptr, &pub);
+    if (rc) return rc;
+    ctx->ctl = reinterpret_cast<Control*>(base + L.ctl);
+    ctx->last_stream = st;
+    ctx->pending = true;
+    ctx->have_events = false;
+    ctx->have_io = false;
+    ctx->last_method = opt.method;
+    ctx->last_collect = false;
+    ctx->stats = ktri_run_stats{};
+    ctx->stats.n = n_total;
+    ctx->stats.nnz = nnz_total;
+    *ctl_out = ctx->ctl;
+    return KTRI_OK;
+}
 
 extern "C" {
 
@@ -1308,10 +1359,8 @@ int ktri_plan_create_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uin
     }
     // occupancy queries happen once, outside the capture
     for (u32 sd : {(u32)ktri::SMALL_D_LOW, (u32)ktri::SMALL_D}) {
-        for (bool w : {false, true}) {
-            (void)ktri::count_grid_auto<u32>(ctx->num_sms, sd, w);
-            (void)ktri::count_grid_auto<u64>(ctx->num_sms, sd, w);
-        }
+        (void)ktri::count_grid_auto<u32>(ctx->num_sms, sd);
+        (void)ktri::count_grid_auto<u64>(ctx->num_sms, sd);
     }
     cudaStream_t cs = nullptr;
     cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);

@@ -14,14 +14,15 @@
 //
 // Three kernels split the owners by out-degree (the bounds are runtime options, at most
 // SMALL_D and MEDIUM_D):
-//   k_count_small: owners with out-degree <= small_outdegree (instantiated for bounds up to
-//     SMALL_D_LOW and up to SMALL_D, both five blocks per SM).  Merge-path tiles over the
-//     adjacency (as in orientation) give every block the same number of slots; the tables of
-//     all owners in a tile live side by side in shared memory.  Selected edges are queued,
-//     counting-sorted by streamed-list length so that the lanes of a warp carry equal work,
-//     then streamed one list per thread with uint4 loads.
-//   k_count_medium: owners up to medium_outdegree, one warp per (owner, segment) tile with
-//     the warp's own table, filter and survivor buffer, so tiles need no block barrier.
+//   k_count_small: owners with out-degree <= small_outdegree and degree <= SMALL_WARP_DEG
+//     (instantiated for bounds up to SMALL_D_LOW and up to SMALL_D).  A warp takes 32
+//     consecutive vertices and counts their owners in groups of up to eight that share its
+//     slice of shared memory: tables side by side, one flattened pass over all their keys, one
+//     over all their adjacency slots (queueing the lower neighbours' lists), a counting sort of
+//     the queue by list length, then one list per lane with uint4 loads.  No block barrier.
+//   k_count_medium: owners up to medium_outdegree (and small-out-degree owners of larger
+//     degree), one warp per (owner, segment) tile with the warp's own table, filter and
+//     survivor buffer, so tiles need no block barrier.
 //   k_count_large: larger owners, one (owner, segment) tile per block iteration.  Short
 //     streamed lists are handled one per thread while the segment is scanned; longer ones are
 //     queued and taken one at a time by whole warps (one entry per lane, eight loads in
@@ -70,6 +71,28 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, u32 p
     return false;
 }
 
+// Loads of the counting bodies.  The standalone kernels read through the read-only path
+// (CG = false): their inputs do not change while they run.  The serving engine (CG = true) runs
+// across many batches whose buffers other kernels rewrite meanwhile, so it reads at L2 only,
+// where those writes are visible, never from lines an SM cached earlier.
+template <bool CG, typename T>
+__device__ __forceinline__ T ld_in(const T* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return __ldg(p);
+}
+template <bool CG, typename OffT>
+__device__ __forceinline__ Desc<OffT> ld_desc(const Desc<OffT>* p) {
+    if constexpr (!CG) {
+        return load_desc(p);
+    } else if constexpr (sizeof(OffT) == 4) {
+        const uint2 v = __ldcg(reinterpret_cast<const uint2*>(p));
+        return Desc<OffT>{v.x, v.y};
+    } else {
+        const uint4 v = __ldcg(reinterpret_cast<const uint4*>(p));
+        return Desc<OffT>{(u64)v.x | ((u64)v.y << 32), v.z, 0};
+    }
+}
+
 // Hit counters of the owners' tables are 16-bit, two per word: a key gets at most one hit per
 // streamed list, and a tile streams at most LARGE_SEG (block and warp kernels) or one tile's
 // slots (small-owner kernel) lists, so they cannot overflow.
@@ -110,338 +133,254 @@ __device__ __forceinline__ u32 bucket_probe16_flat(const u32* keys, u32* hits32,
     return slot < 4u ? 1u : 0u;
 }
 
-template <int BLOCK, int IPT, int SD, typename OffT>
-struct SmallLayout {
-    static constexpr int TILE = BLOCK * IPT;
-    static constexpr int TBL = 4 * (TILE + 2 * SD);  // sum of per-owner table sizes (pow2 >= max(4, 2d) <= 4d)
-    static constexpr int WPT = (TILE + 1 + BLOCK - 1) / BLOCK;
-    static_assert(TILE < 65536, "window offsets and hit counters are 16-bit");
-    static constexpr size_t off_fo = 0;  // first_out of the window, clamped to the tile, relative to its first slot
-    static constexpr size_t off_desc = align16(off_fo + sizeof(unsigned short) * (TILE + 2));
-    static constexpr size_t off_tb = align16(off_desc + sizeof(Desc<OffT>) * (TILE + 2));
-    // key offsets of the owners while the tables are filled, then the owners' hit totals
-    static constexpr size_t off_ko = align16(off_tb + sizeof(u32) * (TILE + 2));
-    static constexpr size_t off_keys = align16(off_ko + sizeof(u32) * (TILE + 2));
-    static constexpr size_t off_hits = align16(off_keys + sizeof(u32) * TBL);  // two u16 counters per word
-    static constexpr size_t off_qy = align16(off_hits + sizeof(u32) * (TBL / 2));
-    static constexpr size_t off_qs = align16(off_qy + sizeof(u32) * TILE);
-    static constexpr size_t off_qm = align16(off_qs + sizeof(OffT) * TILE);
-    static constexpr size_t off_ord = align16(off_qm + sizeof(unsigned short) * TILE);
-    static constexpr size_t bytes = align16(off_ord + sizeof(unsigned short) * TILE);
+// Small owners (k_count_small), warp-granular.  A warp takes
+// 32 consecutive vertices at a time and counts their owners (out-degree 1..small_outdegree,
+// degree at most SMALL_WARP_DEG; owners of larger degree go to the medium kernel's tiles) in
+// groups: up to GROUP owners whose tables fit TAB slots and whose adjacency fits QCAP slots
+// share the warp's slice of shared memory.  Each phase runs over the whole group at once (all
+// keys, then all adjacency slots, then all queued lists), so one round of global loads serves
+// every owner of the group; the queue is counting-sorted by list length and streamed one list
+// per lane, longest first.  Only __syncwarp orders the phases: the warps of a block never wait
+// for one another.
+template <int SD, typename OffT>
+struct SmallWarpLayout {
+    static constexpr int GROUP = 8;      // owners per group
+    static constexpr int TAB = 256;      // table slots of a group (each table a power of two >= 2 d+)
+    static constexpr int QCAP = 256;     // adjacency slots of a group (the queue's capacity)
+    static constexpr int NBIN = SD + 2;  // list lengths 0..SD
+    static constexpr int OW = 10;        // words per owner record
+    // u32 words per warp
+    static constexpr int W_KEYS = 0;
+    static constexpr int W_HITS = W_KEYS + TAB;                         // two 16-bit counters per word
+    static constexpr int W_QY = W_HITS + TAB / 2;
+    static constexpr int W_QS = W_QY + QCAP;                            // list starts (OffT)
+    static constexpr int W_QM = W_QS + QCAP * (int)(sizeof(OffT) / 4);  // (owner << 8) | length
+    static constexpr int W_ORD = W_QM + QCAP;                           // queue order by length (u16)
+    static constexpr int W_BIN = W_ORD + QCAP / 2;                      // 64 length bins
+    static constexpr int W_OWN = W_BIN + 64;
+    static constexpr int PER_WARP = (W_OWN + OW * GROUP + 3) & ~3;
+    static constexpr size_t bytes(int warps) { return sizeof(u32) * PER_WARP * warps; }
 };
 
-template <int BLOCK, int IPT, int SD, typename OffT>
-__global__ void __launch_bounds__(BLOCK, 5) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
-                                                       u64 n, u64 nnz, const Desc<OffT>* __restrict__ vdesc,
-                                                       const u32* __restrict__ headp,
-                                                       const u32* __restrict__ tile_i0, u32 sd,
-                                                       u64* __restrict__ cnt, u64* __restrict__ partials,
-                                                       Control* ctl) {
-    using L = SmallLayout<BLOCK, IPT, SD, OffT>;
-    static_assert(L::TILE == TILE_BASE, "one counting tile = one base tile");
-    constexpr int TILE = L::TILE;
-    constexpr int WPT = L::WPT;
-    static_assert(SD < 64, "list length is packed in 6 bits");
-    static_assert(TILE + 2 <= 1024, "window owner index is packed in 10 bits");
-    extern __shared__ __align__(16) unsigned char smem[];
-    unsigned short* s_fo = reinterpret_cast<unsigned short*>(smem + L::off_fo);
-    Desc<OffT>* s_desc = reinterpret_cast<Desc<OffT>*>(smem + L::off_desc);
-    u32* s_tb = reinterpret_cast<u32*>(smem + L::off_tb);
-    u32* s_ko = reinterpret_cast<u32*>(smem + L::off_ko);
-    u32* s_own = reinterpret_cast<u32*>(smem + L::off_ko);  // after the tables are filled
-    u32* s_keys = reinterpret_cast<u32*>(smem + L::off_keys);
-    u32* s_hits = reinterpret_cast<u32*>(smem + L::off_hits);
-    u32* q_y = reinterpret_cast<u32*>(smem + L::off_qy);
-    OffT* q_s = reinterpret_cast<OffT*>(smem + L::off_qs);
-    unsigned short* q_m = reinterpret_cast<unsigned short*>(smem + L::off_qm);  // (owner << 6) | list length
-    unsigned short* q_ord = reinterpret_cast<unsigned short*>(smem + L::off_ord);
-    __shared__ u32 s_warp[BLOCK / 32];
-    __shared__ u64 s_red[BLOCK / 32];
-    __shared__ u64 s_b[3];
-    __shared__ u32 s_bins[SD + 2];
-    __shared__ u32 s_qn, s_chunk;
-
-    if (ctl->err & DEV_ERR_MASK) return;
+// One batch of 32 consecutive vertices (bi), counted by one warp in its slice of shared
+// memory: the owners among them, in groups.
+template <int SD, typename OffT, bool CG = false>
+__device__ __forceinline__ void small_batch(u32* base, u64 bi, const u64* __restrict__ fo,
+                                            const u32* __restrict__ head, u64 n,
+                                            const Desc<OffT>* __restrict__ vdesc, const u32* __restrict__ headp,
+                                            u32 sd, u64* __restrict__ cnt, u64& local_total, u32& dup) {
+    using L = SmallWarpLayout<SD, OffT>;
+    constexpr int OW = L::OW;
+    static_assert(2 * SD <= L::TAB / 2, "two owners of the largest out-degree fit a group's tables");
+    static_assert(SMALL_WARP_DEG <= (u32)L::QCAP, "one owner's adjacency fits the queue");
+    static_assert(SD < 256 && L::NBIN <= 64, "list length is packed in 8 bits, bins two per lane");
     const int lane = threadIdx.x & 31;
-    const u64 total_items = n + nnz;
-    const u64 ntiles = (total_items + TILE - 1) / TILE;
+    const u32 lt_mask = (1u << lane) - 1;
+    u32* keys = base + L::W_KEYS;
+    u32* hitc = base + L::W_HITS;
+    u32* q_y = base + L::W_QY;
+    OffT* q_s = reinterpret_cast<OffT*>(base + L::W_QS);
+    u32* q_m = base + L::W_QM;
+    unsigned short* q_ord = reinterpret_cast<unsigned short*>(base + L::W_ORD);
+    u32* bins = base + L::W_BIN;
+    // owner gi at own + OW * gi: [0] vertex, [1] (table offset << 5) | lg, [2] out-degree,
+    // [3] key prefix, [4] adjacency prefix, [5] hit total, [6..7] first adjacency slot (u64),
+    // [8..9] out-list start (u64)
+    u32* own = base + L::W_OWN;
     const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
-    u64 local_total = 0;
-    u32 dup = 0;
-
-    while (true) {
-        if (threadIdx.x == 0) {
-            const u64 t = atomicAdd(&ctl->small_next, 1ull);
-            s_b[2] = t;
-            if (t < ntiles) {
-                s_b[0] = tile_i0[t];
-                s_b[1] = tile_i0[t + 1];
-            }
-            s_qn = 0;
-            s_chunk = 0;
-        }
-        if (threadIdx.x < SD + 2) s_bins[threadIdx.x] = 0;
-        __syncthreads();
-        const u64 tile = s_b[2];
-        if (tile >= ntiles) break;
-        const u64 d0 = tile * TILE;
-        const u64 d1 = d0 + TILE < total_items ? d0 + TILE : total_items;
-        const u64 i0 = s_b[0], i1 = s_b[1];
-        if (i0 >= n) {  // only trailing vertex-end events: nothing to count
-            __syncthreads();
-            continue;
-        }
-        const u64 j0 = d0 - i0, j1 = d1 - i1;
-        const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
-        const u32 nw = (u32)(fo_last - i0);  // window vertices [i0, fo_last)
-        for (u32 k = threadIdx.x; k <= nw; k += BLOCK) {
-            u64 f = fo[i0 + k];
-            f = f < j0 ? j0 : (f > j1 ? j1 : f);
-            s_fo[k] = (unsigned short)(f - j0);
-        }
-        for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
-            s_desc[k] = load_desc(vdesc + i0 + k);
-        }
-        __syncthreads();
-
-        // table sizes and key offsets of the owners in the window
-        u32 packed[WPT];
-        u32 tsum = 0;
+    const u64 v = bi * 32 + lane;
+    Desc<OffT> dv;
+    dv.start = 0;
+    dv.d = 0;
+    u64 a = 0;
+    u32 deg = 0;
+    bool is_owner = false;
+    if (v < n) {
+        dv = ld_desc<CG>(vdesc + v);
+        a = ld_in<CG>(fo + v);
+        const u64 b = ld_in<CG>(fo + v + 1);
+        is_owner = dv.d > 0 && dv.d <= sd && b - a <= (u64)SMALL_WARP_DEG;
+        deg = (u32)(b - a);
+    }
+    u32 lg = 0, tsz = 0;
+    if (is_owner) {
+        lg = ceil_log2(2 * dv.d);
+        if (lg < 2) lg = 2;
+        tsz = 1u << lg;
+    }
+    u32 todo = __ballot_sync(0xFFFFFFFFu, is_owner);
+    while (todo) {
+        // the group: the next owners in lane order while their tables and adjacency fit
+        const bool cand = (todo >> lane) & 1u;
+        u32 pk = cand ? (tsz << 16) | deg : 0u;  // inclusive prefix of (table slots, adjacency)
 #pragma unroll
-        for (int r = 0; r < WPT; ++r) {
-            const u32 k = threadIdx.x * WPT + r;
-            packed[r] = 0;
-            if (k < nw) {
-                const u32 d = s_desc[k].d;
-                if (s_fo[k] < s_fo[k + 1] && d > 0 && d <= sd) {
-                    u32 lg = ceil_log2(2 * d);
-                    if (lg < 2) lg = 2;
-                    packed[r] = ((1u << lg) << 16) | d;
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xFFFFFFFFu, pk, o);
+            if (lane >= o) pk += y;
+        }
+        const u32 rank = __popc(todo & lt_mask);
+        const bool in = cand && (pk >> 16) <= (u32)L::TAB && (pk & 0xFFFFu) <= (u32)L::QCAP &&
+                        rank < (u32)L::GROUP;
+        const u32 gmask = __ballot_sync(0xFFFFFFFFu, in);
+        todo &= ~gmask;
+        const u32 G = __popc(gmask);
+        const u32 last = 31 - __clz(gmask);  // the group's last member holds its totals
+        const u32 tot_pk = __shfl_sync(0xFFFFFFFFu, pk, last);
+        const u32 T = tot_pk >> 16, D = tot_pk & 0xFFFFu;
+        u32 kk = in ? dv.d : 0u;  // inclusive prefix of the members' out-degrees
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xFFFFFFFFu, kk, o);
+            if (lane >= o) kk += y;
+        }
+        const u32 K = __shfl_sync(0xFFFFFFFFu, kk, last);
+        if (in) {
+            const u32 gi = __popc(gmask & lt_mask);
+            u32* o = own + OW * gi;
+            const u64 ls = list_start(dv);
+            o[0] = (u32)v;
+            o[1] = (((pk >> 16) - tsz) << 5) | lg;
+            o[2] = dv.d;
+            o[3] = kk - dv.d;
+            o[4] = (pk & 0xFFFFu) - deg;
+            o[5] = 0;
+            o[6] = (u32)a;
+            o[7] = (u32)(a >> 32);
+            o[8] = (u32)ls;
+            o[9] = (u32)(ls >> 32);
+        }
+        for (u32 i = lane; i < T; i += 32) keys[i] = EMPTY_KEY;
+        for (u32 i = lane; i < T / 2; i += 32) hitc[i] = 0;
+        for (u32 i = lane; i < 64; i += 32) bins[i] = 0;
+        __syncwarp();
+        // keys of every owner of the group
+        for (u32 q = lane; q < K; q += 32) {
+            u32 gi = 0;
+#pragma unroll
+            for (int g = 1; g < L::GROUP; ++g)
+                if ((u32)g < G && own[OW * g + 3] <= q) gi = g;
+            const u32* o = own + OW * gi;
+            const u64 xs = (u64)o[8] | ((u64)o[9] << 32);
+            if (!bucket_insert(keys + (o[1] >> 5), o[1] & 31u, ld_in<CG>(headp + xs + (q - o[3])))) dup = 1;
+        }
+        // adjacency of every owner: queue the lower neighbours' lists (four slots in flight)
+        u32 qn = 0;
+        for (u32 e0 = 0; e0 < D; e0 += 128) {
+            u32 yv[4], gv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const u32 e = e0 + 32 * u + lane;
+                yv[u] = NONE;
+                gv[u] = 0;
+                if (e < D) {
+                    u32 gi = 0;
+#pragma unroll
+                    for (int g = 1; g < L::GROUP; ++g)
+                        if ((u32)g < G && own[OW * g + 4] <= e) gi = g;
+                    const u64 xa = (u64)own[OW * gi + 6] | ((u64)own[OW * gi + 7] << 32);
+                    gv[u] = gi;
+                    yv[u] = ld_in<CG>(head + xa + (e - own[OW * gi + 4]));
                 }
             }
-            tsum += packed[r];
-        }
-        u32 ptot;
-        u32 pbase = block_exclusive_scan<BLOCK>(tsum, s_warp, &ptot);
+            Desc<OffT> dyv[4];
 #pragma unroll
-        for (int r = 0; r < WPT; ++r) {
-            const u32 k = threadIdx.x * WPT + r;
-            if (k < nw) {
-                const u32 p = packed[r];
-                if (p) {
-                    const u32 sz = p >> 16;
-                    s_tb[k] = ((pbase >> 16) << 5) | (31 - __clz(sz));
-                } else {
-                    s_tb[k] = NONE;
+            for (int u = 0; u < 4; ++u) {
+                dyv[u].start = 0;
+                dyv[u].d = 0;
+                if (yv[u] < n) dyv[u] = ld_desc<CG>(vdesc + yv[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const u32 gi = gv[u], dy = dyv[u].d;
+                const bool sel = yv[u] < n && dy > 0 && key_less(dy, yv[u], own[OW * gi + 2], own[OW * gi]);
+                const u32 ball = __ballot_sync(0xFFFFFFFFu, sel);
+                if (sel) {
+                    const u32 qi = qn + __popc(ball & lt_mask);
+                    q_y[qi] = yv[u];
+                    q_s[qi] = (OffT)list_group(dyv[u]);
+                    q_m[qi] = (gi << 8) | dy;
+                    atomicAdd(&bins[dy], 1u);
                 }
-                s_ko[k] = pbase & 0xFFFFu;
+                qn += __popc(ball);
             }
-            pbase += packed[r];
         }
-        const u32 table_slots = ptot >> 16, nkeys = ptot & 0xFFFFu;
-        if (threadIdx.x == 0) s_ko[nw] = nkeys;
-        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) s_keys[s] = EMPTY_KEY;
-        for (u32 s = threadIdx.x; s < table_slots / 2; s += BLOCK) s_hits[s] = 0;
-        __syncthreads();
-
-        // insert the out-lists of the owners (one key per thread per step)
-        for (u32 q = threadIdx.x; q < nkeys; q += BLOCK) {
-            u32 lo = 0, hi = nw - 1;
-            while (lo < hi) {
-                u32 mid = (lo + hi + 1) >> 1;
-                if (s_ko[mid] <= q) lo = mid; else hi = mid - 1;
-            }
-            const u32 tb = s_tb[lo];
-            const u32 w = __ldg(headp + list_start(s_desc[lo]) + (q - s_ko[lo]));
-            if (!bucket_insert(s_keys + (tb >> 5), tb & 31u, w)) dup = 1;
-        }
-
-        // walk this thread's items of the merge path and queue the edges this tile owns
-        const u64 dt = d0 + (u64)threadIdx.x * IPT < d1 ? d0 + (u64)threadIdx.x * IPT : d1;
-        const u64 dte = dt + IPT < d1 ? dt + IPT : d1;
-        // merge-path search in the window: largest i in [i0, i1] with first_out[i] + i <= dt
-        u64 i_start;
+        __syncwarp();
+        // counting sort of the queue by list length (bins 2 lane and 2 lane + 1 in each lane)
         {
-            u64 lo = i0, hi = i1;
-            while (lo < hi) {
-                const u64 mid = (lo + hi + 1) >> 1;
-                if ((u64)s_fo[mid - i0] + j0 + mid <= dt) lo = mid; else hi = mid - 1;
-            }
-            i_start = lo;
-        }
-        u32 own[IPT], yv[IPT];
-        {
-            u64 i = i_start;
-            u32 j = (u32)(dt - i_start - j0);  // slot relative to the tile's first slot
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                own[k] = NONE;
-                yv[k] = 0;
-                if (dt + k < dte) {
-                    if (i < n && j < s_fo[i + 1 - i0]) {
-                        const u32 o = (u32)(i - i0);
-                        const u32 d = s_desc[o].d;
-                        if (d > 0 && d <= sd) {
-                            own[k] = o;
-                            yv[k] = __ldg(head + j0 + j);
-                        }
-                        ++j;
-                    } else {
-                        ++i;
-                    }
-                }
-            }
-        }
-        Desc<OffT> vy[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            vy[k].start = 0;
-            vy[k].d = 0;
-            if (own[k] != NONE && yv[k] < n) vy[k] = load_desc(vdesc + yv[k]);
-        }
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            const u32 o = own[k];
-            bool sel = false;
-            if (o != NONE) {
-                const u32 dy = vy[k].d;
-                sel = dy > 0 && key_less(dy, yv[k], s_desc[o].d, i0 + o);
-            }
-            const u32 ball = __ballot_sync(0xFFFFFFFFu, sel);
-            u32 base = 0;
-            if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (sel) {
-                const u32 qi = base + __popc(ball & ((1u << lane) - 1));
-                q_y[qi] = yv[k];
-                q_s[qi] = (OffT)list_group(vy[k]);
-                q_m[qi] = (unsigned short)((o << 6) | vy[k].d);
-                atomicAdd(&s_bins[vy[k].d], 1u);
-            }
-        }
-        __syncthreads();
-
-        // counting sort of the queue by list length; the key offsets are no longer needed and
-        // their words become the owners' hit totals
-        for (u32 k = threadIdx.x; k < nw; k += BLOCK) s_own[k] = 0;
-        const u32 qn = s_qn;
-        if (threadIdx.x < 32) {
-            u32 c0 = s_bins[lane], c1 = lane + 32 < SD + 2 ? s_bins[lane + 32] : 0;
-            u32 x0 = c0;
+            const u32 c0 = bins[2 * lane], c1 = bins[2 * lane + 1];
+            u32 x = c0 + c1;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                u32 y = __shfl_up_sync(0xFFFFFFFFu, x0, o);
-                if (lane >= o) x0 += y;
+                const u32 y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
             }
-            const u32 tot0 = __shfl_sync(0xFFFFFFFFu, x0, 31);
-            u32 x1 = c1;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                u32 y = __shfl_up_sync(0xFFFFFFFFu, x1, o);
-                if (lane >= o) x1 += y;
-            }
-            s_bins[lane] = x0 - c0;
-            if (lane + 32 < SD + 2) s_bins[lane + 32] = tot0 + x1 - c1;
+            bins[2 * lane] = x - c0 - c1;
+            bins[2 * lane + 1] = x - c1;
         }
-        __syncthreads();
-        for (u32 qi = threadIdx.x; qi < qn; qi += BLOCK) {
-            const u32 pos = atomicAdd(&s_bins[q_m[qi] & 63u], 1u);
-            q_ord[pos] = (unsigned short)qi;
-        }
-        __syncthreads();
-
-        // stream the queued lists: warps take chunks of 32 from the length-sorted queue, longest
-        // first, so the lanes of a warp carry equal lengths and the warps finish together
-        while (true) {
-            u32 c32 = 0;
-            if (lane == 0) c32 = atomicAdd(&s_chunk, 32u);
-            c32 = __shfl_sync(0xFFFFFFFFu, c32, 0);
-            if (c32 >= qn) break;
-            const u32 r = c32 + lane;
-            if (r >= qn) continue;
+        __syncwarp();
+        for (u32 qi = lane; qi < qn; qi += 32) q_ord[atomicAdd(&bins[q_m[qi] & 0xFFu], 1u)] = (unsigned short)qi;
+        __syncwarp();
+        // stream the queued lists, one per lane, longest first
+        for (u32 r = lane; r < qn; r += 32) {
             const u32 qi = q_ord[qn - 1 - r];
             const u32 meta = q_m[qi];
-            const u32 o = meta >> 6, dy = meta & 63u;
-            const u32 tb = s_tb[o];
-            const u32* keys = s_keys + (tb >> 5);
-            u32* hitc = s_hits + ((tb >> 5) >> 1);  // table offsets are multiples of 4 slots
-            const u32 lg = tb & 31u;
+            const u32 gi = meta >> 8, dy = meta & 0xFFu;
+            const u32 tb = own[OW * gi + 1];
+            const u32* tk = keys + (tb >> 5);
+            u32* th = hitc + ((tb >> 5) >> 1);  // table offsets are multiples of 4 slots
+            const u32 tl = tb & 31u;
             const u64 q0 = (u64)q_s[qi];
             u32 hits = 0;
-            // the list's 16-byte groups are loaded PRE at a time before any probe, so their
-            // latencies overlap instead of adding up
-            constexpr int PRE = 4;
-#pragma unroll 1
-            for (int c0 = 0; c0 < SD / 4; c0 += PRE) {
-                if (4 * c0 >= (int)dy) break;
-                uint4 qv[PRE];
+            for (u32 g0 = 0; 4 * g0 < dy; g0 += 4) {
+                uint4 qv[4];
 #pragma unroll
-                for (int c = 0; c < PRE; ++c)
-                    qv[c] = 4 * (c0 + c) < (int)dy ? __ldg(headp4 + q0 + c0 + c)
-                                                   : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+                for (int c = 0; c < 4; ++c)
+                    qv[c] = 4 * (g0 + c) < dy ? ld_in<CG>(headp4 + q0 + g0 + c)
+                                              : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
 #pragma unroll
-                for (int c = 0; c < PRE; ++c) {
-                    const int e = 4 * (c0 + c);
-                    if (e < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
-                    if (e + 1 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
-                    if (e + 2 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
-                    if (e + 3 < (int)dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
+                for (int c = 0; c < 4; ++c) {
+                    const u32 e = 4 * (g0 + c);
+                    if (e < dy) hits += bucket_probe16(tk, th, tl, qv[c].x);
+                    if (e + 1 < dy) hits += bucket_probe16(tk, th, tl, qv[c].y);
+                    if (e + 2 < dy) hits += bucket_probe16(tk, th, tl, qv[c].z);
+                    if (e + 3 < dy) hits += bucket_probe16(tk, th, tl, qv[c].w);
                 }
             }
             if (hits) {
                 atomicAdd(&cnt[q_y[qi]], (u64)hits);
-                atomicAdd(&s_own[o], hits);
+                atomicAdd(&own[OW * gi + 5], hits);
             }
         }
-        __syncthreads();
-
-        // flush: hits of every key (vertex w), then the owners' own counts
-        for (u32 s = threadIdx.x; s < table_slots; s += BLOCK) {
-            const u32 h = read16(s_hits, s);
-            if (h) atomicAdd(&cnt[s_keys[s]], (u64)h);
+        __syncwarp();
+        // flush: every key's hits, then the owners' totals
+        for (u32 i = lane; i < T; i += 32) {
+            const u32 h = read16(hitc, i);
+            if (h) atomicAdd(&cnt[keys[i]], (u64)h);
         }
-        for (u32 k = threadIdx.x; k < nw; k += BLOCK) {
-            const u32 t = s_own[k];
+        if ((u32)lane < G) {
+            const u32 t = own[OW * lane + 5];
             if (t) {
-                atomicAdd(&cnt[i0 + k], (u64)t);
+                atomicAdd(&cnt[own[OW * lane]], (u64)t);
                 local_total += t;
             }
         }
-        __syncthreads();
+        __syncwarp();  // the next group reuses the slice only after every lane has flushed
     }
-    if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
-    const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
-    if (threadIdx.x == 0) partials[blockIdx.x] = bt;
 }
 
-// Small owners, one warp per owner (the form used when Options.small_kernel selects it): a
-// warp takes 32 consecutive vertices at a time and, for each owner among them (out-degree
-// 1..small_outdegree, degree at most SMALL_WARP_DEG; owners of larger degree go to the medium
-// kernel's tiles), fills its own slice of shared memory with the owner's table and streams the
-// out-list of every lower neighbour through it, one list per lane.  No block barrier: the warps
-// of a block never wait for one another.
-template <int SD>
-struct SmallWarpLayout {
-    static constexpr int TS = SD <= 32 ? 64 : 128;  // table slots: a power of two >= 2 * SD
-    static constexpr int PER_WARP = TS + TS / 2;     // keys, then two 16-bit hit counters per word
-};
-
 template <int BLOCK, int SD, typename OffT>
-__global__ void __launch_bounds__(BLOCK, 4) k_count_small_warp(const u64* __restrict__ fo, const u32* __restrict__ head,
-                                                            u64 n, const Desc<OffT>* __restrict__ vdesc,
-                                                            const u32* __restrict__ headp, u32 sd,
-                                                            u64* __restrict__ cnt, u64* __restrict__ partials,
-                                                            Control* ctl) {
-    using L = SmallWarpLayout<SD>;
+__global__ void __launch_bounds__(BLOCK, 4) k_count_small(const u64* __restrict__ fo, const u32* __restrict__ head,
+                                                          u64 n, const Desc<OffT>* __restrict__ vdesc,
+                                                          const u32* __restrict__ headp, u32 sd,
+                                                          u64* __restrict__ cnt, u64* __restrict__ partials,
+                                                          Control* ctl) {
+    using L = SmallWarpLayout<SD, OffT>;
     constexpr int NW = BLOCK / 32;
-    static_assert(2 * SD <= L::TS, "a table holds twice the owner's keys");
-    __shared__ __align__(16) u32 s_tab[NW * L::PER_WARP];
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ u64 s_red[NW];
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    u32* keys = s_tab + warp * L::PER_WARP;
-    u32* hitc = keys + L::TS;
-    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    u32* base = reinterpret_cast<u32*>(smem) + warp * L::PER_WARP;
     const u64 nbatch = (n + 31) / 32;
     u64 local_total = 0;
     u32 dup = 0;
@@ -450,81 +389,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_count_small_warp(const u64* __rest
         if (lane == 0) bi = atomicAdd(&ctl->small_next, 1ull);
         bi = __shfl_sync(0xFFFFFFFFu, bi, 0);
         if (bi >= nbatch) break;
-        const u64 v = bi * 32 + lane;
-        Desc<OffT> dv;
-        dv.start = 0;
-        dv.d = 0;
-        u64 a = 0, b = 0;
-        bool own = false;
-        if (v < n) {
-            dv = load_desc(vdesc + v);
-            a = fo[v];
-            b = fo[v + 1];
-            own = dv.d > 0 && dv.d <= sd && b - a <= (u64)SMALL_WARP_DEG;
-        }
-        const u64 vs = list_start(dv);
-        u32 todo = __ballot_sync(0xFFFFFFFFu, own);
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const u64 x = bi * 32 + src;
-            const u32 dx = __shfl_sync(0xFFFFFFFFu, dv.d, src);
-            const u64 xs = __shfl_sync(0xFFFFFFFFu, vs, src);
-            const u64 xa = __shfl_sync(0xFFFFFFFFu, a, src);
-            const u32 xdeg = (u32)(__shfl_sync(0xFFFFFFFFu, b, src) - xa);
-            u32 lg = ceil_log2(2 * dx);
-            if (lg < 2) lg = 2;
-            const u32 size = 1u << lg;
-            for (u32 i = lane; i < size; i += 32) keys[i] = EMPTY_KEY;
-            for (u32 i = lane; i < size / 2; i += 32) hitc[i] = 0;
-            __syncwarp();
-            for (u32 q = lane; q < dx; q += 32)
-                if (!bucket_insert(keys, lg, __ldg(headp + xs + q))) dup = 1;
-            __syncwarp();
-            u32 T = 0;
-            for (u32 e0 = 0; e0 < xdeg; e0 += 32) {
-                u32 hits = 0;
-                if (e0 + lane < xdeg) {
-                    const u32 y = __ldg(head + xa + e0 + lane);
-                    if (y < n) {
-                        const Desc<OffT> vy = load_desc(vdesc + y);
-                        const u32 dy = vy.d;
-                        if (dy > 0 && key_less(dy, y, dx, x)) {
-                            // the list's 16-byte groups, four loads in flight before the probes
-                            const u64 q0 = list_group(vy);
-                            for (u32 g0 = 0; 4 * g0 < dy; g0 += 4) {
-                                uint4 qv[4];
-#pragma unroll
-                                for (int c = 0; c < 4; ++c)
-                                    qv[c] = 4 * (g0 + c) < dy ? __ldg(headp4 + q0 + g0 + c)
-                                                              : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
-#pragma unroll
-                                for (int c = 0; c < 4; ++c) {
-                                    const u32 e = 4 * (g0 + c);
-                                    if (e < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].x);
-                                    if (e + 1 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].y);
-                                    if (e + 2 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].z);
-                                    if (e + 3 < dy) hits += bucket_probe16(keys, hitc, lg, qv[c].w);
-                                }
-                            }
-                            if (hits) atomicAdd(&cnt[y], (u64)hits);
-                        }
-                    }
-                }
-                T += hits;
-            }
-            __syncwarp();
-            for (u32 i = lane; i < size; i += 32) {
-                const u32 h = read16(hitc, i);
-                if (h) atomicAdd(&cnt[keys[i]], (u64)h);
-            }
-            T = __reduce_add_sync(0xFFFFFFFFu, T);
-            if (lane == 0 && T) {
-                atomicAdd(&cnt[x], (u64)T);
-                local_total += T;
-            }
-            __syncwarp();  // the next owner clears the table only after every lane has flushed
-        }
+        small_batch<SD, OffT>(base, bi, fo, head, n, vdesc, headp, sd, cnt, local_total, dup);
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
     const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
@@ -542,7 +407,12 @@ struct LargeLayout {
     static constexpr size_t off_wbuf = align16(off_filt + sizeof(u32) * FWORDS);
     static constexpr size_t off_qy = align16(off_wbuf + sizeof(u32) * WBUF * (BLOCK / 32));
     static constexpr size_t off_qd = align16(off_qy + sizeof(u32) * LARGE_SEG);
-    static constexpr size_t bytes = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
+    // block scalars: reduction slots, queue length and cursor, the bulk copy's mbarrier
+    static constexpr size_t off_red = align16(off_qd + sizeof(Desc<OffT>) * LARGE_SEG);
+    static constexpr size_t off_qn = off_red + sizeof(u64) * (BLOCK / 32);
+    static constexpr size_t off_next = off_qn + sizeof(u32);
+    static constexpr size_t off_bar = align16(off_next + sizeof(u32));
+    static constexpr size_t bytes = align16(off_bar + sizeof(unsigned long long));
 };
 
 // One-hash membership filter of the owner's keys (2^fl bits): a clear bit is a sure miss.
@@ -555,7 +425,7 @@ __device__ __forceinline__ bool filter_test(const u32* filt, u32 fl, u32 w) {
 // A whole warp streams one list (d entries at lst) through the owner's filter and table.
 // Entries that pass the filter are packed into the warp's buffer (64 entries) and looked up
 // 32 at a time.  Returns this lane's share of the hits.
-template <int U>
+template <int U, bool CG = false>
 __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32 d, const u32* keys, u32* hitc, u32 lg,
                                                 const u32* filt, u32 fl, u32* wbuf, int lane, u32 lt_mask) {
     u32 hits = 0, nbuf = 0;
@@ -566,7 +436,7 @@ __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32
     for (u32 p0 = 0; p0 < d; p0 += 32 * U, lp += 32 * U, rem -= 32 * U) {
         u32 w[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) w[u] = rem > 32 * u ? __ldg(lp + 32 * u) : EMPTY_KEY;
+        for (int u = 0; u < U; ++u) w[u] = rem > 32 * u ? ld_in<CG>(lp + 32 * u) : EMPTY_KEY;
         const int left = (int)(d - p0);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -597,7 +467,7 @@ __device__ __forceinline__ u32 warp_stream_list(const u32* __restrict__ lst, u32
 
 // A lane streams one short list (d <= LONG_LIST entries, 16-byte aligned) through the owner's
 // filter and table.
-template <typename OffT>
+template <typename OffT, bool CG = false>
 __device__ __forceinline__ u32 lane_stream_short(const uint4* __restrict__ headp4, const Desc<OffT>& vy,
                                                  const u32* keys, u32* hitc, u32 lg, const u32* filt, u32 fl) {
     const u32 dy = vy.d;
@@ -605,7 +475,7 @@ __device__ __forceinline__ u32 lane_stream_short(const uint4* __restrict__ headp
     uint4 qv[LONG_LIST / 4];
 #pragma unroll
     for (int c = 0; c < LONG_LIST / 4; ++c)
-        qv[c] = 4 * c < (int)dy ? __ldg(headp4 + q0 + c) : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
+        qv[c] = 4 * c < (int)dy ? ld_in<CG>(headp4 + q0 + c) : make_uint4(EMPTY_KEY, EMPTY_KEY, EMPTY_KEY, EMPTY_KEY);
     u32 hits = 0;
 #pragma unroll
     for (int c = 0; c < LONG_LIST / 4; ++c) {
@@ -632,6 +502,148 @@ __device__ __forceinline__ void chunk_sizes(u32 klen, u32 max_lg, u32 max_fl, u3
     *fl = f;
 }
 
+// One (owner, segment) tile of a large owner, counted by the whole block.  Returns true when a
+// bounded wait for a bulk copy ran out (inflight: the second wait ran out too).
+template <int BLOCK, int CAP, typename OffT, bool CG = false>
+__device__ __forceinline__ bool large_tile(unsigned char* smem, uint2 tl, const u64* __restrict__ fo,
+                                           const u32* __restrict__ head, u64 n, const Desc<OffT>* __restrict__ vdesc,
+                                           const u32* __restrict__ headp, u32 seg, u64* __restrict__ cnt,
+                                           u32 first_wait_polls, u32& phase, bool& inflight, u64& local_total,
+                                           u32& dup) {
+    using L = LargeLayout<BLOCK, CAP, OffT>;
+    constexpr int NW = BLOCK / 32;
+    constexpr int U = 8;  // loads in flight per lane and list
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u32 lt_mask = (1u << lane) - 1;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    u32* keys = reinterpret_cast<u32*>(smem + L::off_keys);
+    u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
+    u32* filt = reinterpret_cast<u32*>(smem + L::off_filt);
+    u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
+    Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
+    // the owner's keys are staged in the queue's descriptor region, which is free until the scan
+    u32* stage = reinterpret_cast<u32*>(smem + L::off_qd);
+    static_assert(sizeof(Desc<OffT>) * LARGE_SEG >= sizeof(u32) * CAP, "staging fits the queue region");
+    u32* wbuf = reinterpret_cast<u32*>(smem + L::off_wbuf) + warp * L::WBUF;
+    u64* s_red = reinterpret_cast<u64*>(smem + L::off_red);
+    u32& s_qn = *reinterpret_cast<u32*>(smem + L::off_qn);
+    u32& s_next = *reinterpret_cast<u32*>(smem + L::off_next);
+    unsigned long long& s_bar = *reinterpret_cast<unsigned long long*>(smem + L::off_bar);
+    bool timed_out = false;
+    const u64 x = tl.x;
+    const Desc<OffT> dxd = ld_desc<CG>(vdesc + x);
+    const u32 dx = dxd.d;
+    const u64 fx1 = ld_in<CG>(fo + x + 1);
+    const u64 a = ld_in<CG>(fo + x) + (u64)tl.y * seg;
+    const u64 b = a + seg < fx1 ? a + seg : fx1;
+    u64 T = 0;
+    for (u32 c0 = 0; c0 < dx; c0 += CAP) {
+        const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
+        u32 lg, fl;
+        chunk_sizes(klen, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FWORDS * 32)), &lg, &fl);
+        const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
+        for (u32 s = threadIdx.x; s < size; s += BLOCK) keys[s] = EMPTY_KEY;
+        for (u32 s = threadIdx.x; s < size / 2; s += BLOCK) hitc[s] = 0;
+        for (u32 s = threadIdx.x; s < fwords; s += BLOCK) filt[s] = 0;
+        if (threadIdx.x == 0) {
+            s_qn = 0;
+            s_next = 0;
+        }
+        fence_proxy_async_smem();  // earlier generic accesses of the staging region come first
+        __syncthreads();
+        // one bulk copy of the chunk's keys (list starts are 16-byte aligned, and the gapped
+        // layout leaves room to round the length up to whole 16-byte groups)
+        if (threadIdx.x == 0) {
+            const u32 bytes = ((klen + 3u) & ~3u) * (u32)sizeof(u32);
+            mbar_expect_tx(&s_bar, bytes);
+            bulk_copy_g2s(stage, headp + list_start(dxd) + c0, bytes, &s_bar);
+        }
+        const bool arrived = mbar_wait_bounded(&s_bar, phase, first_wait_polls);
+        if (__syncthreads_or(!arrived)) {  // the same decision in every thread
+            // give the copy in flight a second bounded wait, so that it does not land in
+            // shared memory after the block has left; then report the timeout (and, if the
+            // copy still has not landed, that it may be in flight as the block leaves)
+            if (!__syncthreads_or(!mbar_wait_bounded(&s_bar, phase, COPY_WAIT_POLLS))) timed_out = true;
+            else timed_out = inflight = true;
+            break;
+        }
+        phase ^= 1u;
+        for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
+            const u32 w = stage[q];
+            if (!bucket_insert(keys, lg, w)) dup = 1;
+            const u32 h = filter_bit(w, fl);
+            atomicOr(&filt[h >> 5], 1u << (h & 31u));
+        }
+        __syncthreads();
+        // scan the segment: short lists now, long lists into the queue
+        for (u64 e0 = a + (u64)warp * 32; e0 < b; e0 += (u64)NW * 32) {
+            const u64 e = e0 + lane;
+            bool queue = false;
+            u32 y = 0;
+            Desc<OffT> vy;
+            vy.start = 0;
+            vy.d = 0;
+            if (e < b) {
+                y = ld_in<CG>(head + e);
+                if (y < n) vy = ld_desc<CG>(vdesc + y);
+                const u32 dy = vy.d;
+                if (dy > 0 && key_less(dy, y, dx, x)) {
+                    if (dy <= (u32)LONG_LIST) {
+                        const u32 hits = lane_stream_short<OffT, CG>(headp4, vy, keys, hitc, lg, filt, fl);
+                        if (hits) {
+                            atomicAdd(&cnt[y], (u64)hits);
+                            T += hits;
+                        }
+                    } else {
+                        queue = true;
+                    }
+                }
+            }
+            const u32 ball = __ballot_sync(0xFFFFFFFFu, queue);
+            u32 base = 0;
+            if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (queue) {
+                const u32 qi = base + __popc(ball & lt_mask);
+                qy[qi] = y;
+                qd[qi] = vy;
+            }
+        }
+        __syncthreads();
+        // long lists: one warp per list, taken from the queue.  Every entry is tested against
+        // the filter; the survivors are packed into the warp's buffer and looked up in the
+        // table 32 at a time, so the lookups run with full warps.
+        const u32 qn = s_qn;
+        while (true) {
+            u32 qi = 0;
+            if (lane == 0) qi = atomicAdd(&s_next, 1u);
+            qi = __shfl_sync(0xFFFFFFFFu, qi, 0);
+            if (qi >= qn) break;
+            const Desc<OffT> vy = qd[qi];
+            u32 hits = warp_stream_list<U, CG>(headp + list_start(vy), vy.d, keys, hitc, lg, filt, fl, wbuf, lane,
+                                           lt_mask);
+            hits = __reduce_add_sync(0xFFFFFFFFu, hits);
+            if (lane == 0 && hits) {
+                atomicAdd(&cnt[qy[qi]], (u64)hits);
+                T += hits;
+            }
+        }
+        __syncthreads();
+        // flush the hits of every key
+        for (u32 s = threadIdx.x; s < size; s += BLOCK) {
+            const u32 h = read16(hitc, s);
+            if (h) atomicAdd(&cnt[keys[s]], (u64)h);
+        }
+        __syncthreads();
+    }
+    const u64 bt = block_sum_u64<BLOCK>(T, s_red);
+    if (threadIdx.x == 0 && bt) {
+        atomicAdd(&cnt[x], bt);
+        local_total += bt;
+    }
+    return timed_out;
+}
+
 template <int BLOCK, int CAP, typename OffT>
 __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ fo, const u32* __restrict__ head,
                                                        u64 n, const Desc<OffT>* __restrict__ vdesc,
@@ -640,153 +652,26 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
                                                        u64* __restrict__ cnt, u64* __restrict__ partials,
                                                        Control* ctl, u32 first_wait_polls) {
     using L = LargeLayout<BLOCK, CAP, OffT>;
-    constexpr int NW = BLOCK / 32;
-    constexpr int U = 8;  // loads in flight per lane and list
     extern __shared__ __align__(16) unsigned char smem[];
-    u32* keys = reinterpret_cast<u32*>(smem + L::off_keys);
-    u32* hitc = reinterpret_cast<u32*>(smem + L::off_hits);
-    u32* filt = reinterpret_cast<u32*>(smem + L::off_filt);
-    u32* qy = reinterpret_cast<u32*>(smem + L::off_qy);
-    Desc<OffT>* qd = reinterpret_cast<Desc<OffT>*>(smem + L::off_qd);
-    __shared__ u64 s_red[NW];
     __shared__ u64 s_t;
-    __shared__ u32 s_qn, s_next;
-    __shared__ __align__(8) unsigned long long s_bar;  // completion of the owner-list bulk copy
+    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem + L::off_bar);  // the bulk copy's barrier
 
     if (ctl->err & DEV_ERR_MASK) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+    if (threadIdx.x == 0) mbar_init(s_bar, 1);
     fence_proxy_async_smem();
     __syncthreads();
     u32 phase = 0;
     bool timed_out = false, inflight = false;
-    // the owner's keys are staged in the queue's descriptor region, which is free until the scan
-    u32* stage = reinterpret_cast<u32*>(smem + L::off_qd);
-    static_assert(sizeof(Desc<OffT>) * LARGE_SEG >= sizeof(u32) * CAP, "staging fits the queue region");
-    u32* wbuf = reinterpret_cast<u32*>(smem + L::off_wbuf) + warp * L::WBUF;
-    const u32 lt_mask = (1u << lane) - 1;
     const u64 ntiles = *(volatile unsigned long long*)&ctl->large_tiles;
-    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
     u64 local_total = 0;
     u32 dup = 0;
-
     while (true) {
         if (threadIdx.x == 0) s_t = atomicAdd(&ctl->large_next, 1ull);
         __syncthreads();
         const u64 t = s_t;
         if (t >= ntiles) break;
-        const uint2 tl = ltiles[t];
-        const u64 x = tl.x;
-        const Desc<OffT> dxd = load_desc(vdesc + x);
-        const u32 dx = dxd.d;
-        const u64 fx1 = fo[x + 1];
-        const u64 a = fo[x] + (u64)tl.y * seg;
-        const u64 b = a + seg < fx1 ? a + seg : fx1;
-        u64 T = 0;
-        for (u32 c0 = 0; c0 < dx; c0 += CAP) {
-            const u32 klen = dx - c0 < (u32)CAP ? dx - c0 : (u32)CAP;
-            u32 lg, fl;
-            chunk_sizes(klen, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FWORDS * 32)), &lg, &fl);
-            const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
-            for (u32 s = threadIdx.x; s < size; s += BLOCK) keys[s] = EMPTY_KEY;
-            for (u32 s = threadIdx.x; s < size / 2; s += BLOCK) hitc[s] = 0;
-            for (u32 s = threadIdx.x; s < fwords; s += BLOCK) filt[s] = 0;
-            if (threadIdx.x == 0) {
-                s_qn = 0;
-                s_next = 0;
-            }
-            fence_proxy_async_smem();  // earlier generic accesses of the staging region come first
-            __syncthreads();
-            // one bulk copy of the chunk's keys (list starts are 16-byte aligned, and the gapped
-            // layout leaves room to round the length up to whole 16-byte groups)
-            if (threadIdx.x == 0) {
-                const u32 bytes = ((klen + 3u) & ~3u) * (u32)sizeof(u32);
-                mbar_expect_tx(&s_bar, bytes);
-                bulk_copy_g2s(stage, headp + list_start(dxd) + c0, bytes, &s_bar);
-            }
-            const bool arrived = mbar_wait_bounded(&s_bar, phase, first_wait_polls);
-            if (__syncthreads_or(!arrived)) {  // the same decision in every thread
-                // give the copy in flight a second bounded wait, so that it does not land in
-                // shared memory after the block has left; then report the timeout (and, if the
-                // copy still has not landed, that it may be in flight as the block leaves)
-                if (!__syncthreads_or(!mbar_wait_bounded(&s_bar, phase, COPY_WAIT_POLLS))) timed_out = true;
-                else timed_out = inflight = true;
-                break;
-            }
-            phase ^= 1u;
-            for (u32 q = threadIdx.x; q < klen; q += BLOCK) {
-                const u32 w = stage[q];
-                if (!bucket_insert(keys, lg, w)) dup = 1;
-                const u32 h = filter_bit(w, fl);
-                atomicOr(&filt[h >> 5], 1u << (h & 31u));
-            }
-            __syncthreads();
-            // scan the segment: short lists now, long lists into the queue
-            for (u64 e0 = a + (u64)warp * 32; e0 < b; e0 += (u64)NW * 32) {
-                const u64 e = e0 + lane;
-                bool queue = false;
-                u32 y = 0;
-                Desc<OffT> vy;
-                vy.start = 0;
-                vy.d = 0;
-                if (e < b) {
-                    y = __ldg(head + e);
-                    if (y < n) vy = load_desc(vdesc + y);
-                    const u32 dy = vy.d;
-                    if (dy > 0 && key_less(dy, y, dx, x)) {
-                        if (dy <= (u32)LONG_LIST) {
-                            const u32 hits = lane_stream_short<OffT>(headp4, vy, keys, hitc, lg, filt, fl);
-                            if (hits) {
-                                atomicAdd(&cnt[y], (u64)hits);
-                                T += hits;
-                            }
-                        } else {
-                            queue = true;
-                        }
-                    }
-                }
-                const u32 ball = __ballot_sync(0xFFFFFFFFu, queue);
-                u32 base = 0;
-                if (lane == 0 && ball) base = atomicAdd(&s_qn, (u32)__popc(ball));
-                base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                if (queue) {
-                    const u32 qi = base + __popc(ball & lt_mask);
-                    qy[qi] = y;
-                    qd[qi] = vy;
-                }
-            }
-            __syncthreads();
-            // long lists: one warp per list, taken from the queue.  Every entry is tested against
-            // the filter; the survivors are packed into the warp's buffer and looked up in the
-            // table 32 at a time, so the lookups run with full warps.
-            const u32 qn = s_qn;
-            while (true) {
-                u32 qi = 0;
-                if (lane == 0) qi = atomicAdd(&s_next, 1u);
-                qi = __shfl_sync(0xFFFFFFFFu, qi, 0);
-                if (qi >= qn) break;
-                const Desc<OffT> vy = qd[qi];
-                u32 hits = warp_stream_list<U>(headp + list_start(vy), vy.d, keys, hitc, lg, filt, fl, wbuf, lane,
-                                               lt_mask);
-                hits = __reduce_add_sync(0xFFFFFFFFu, hits);
-                if (lane == 0 && hits) {
-                    atomicAdd(&cnt[qy[qi]], (u64)hits);
-                    T += hits;
-                }
-            }
-            __syncthreads();
-            // flush the hits of every key
-            for (u32 s = threadIdx.x; s < size; s += BLOCK) {
-                const u32 h = read16(hitc, s);
-                if (h) atomicAdd(&cnt[keys[s]], (u64)h);
-            }
-            __syncthreads();
-        }
-        const u64 bt = block_sum_u64<BLOCK>(T, s_red);
-        if (threadIdx.x == 0 && bt) {
-            atomicAdd(&cnt[x], bt);
-            local_total += bt;
-        }
+        timed_out = large_tile<BLOCK, CAP, OffT>(smem, ltiles[t], fo, head, n, vdesc, headp, seg, cnt,
+                                                 first_wait_polls, phase, inflight, local_total, dup);
         if (timed_out) break;
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
@@ -807,6 +692,93 @@ struct MediumLayout {
     static constexpr size_t bytes = sizeof(u32) * PER_WARP * NW;
 };
 
+// One (owner, segment) tile of a medium owner, counted by one warp in its slice of shared
+// memory (keys at `keys`, then the hit counters, the filter and the survivor buffer).
+template <int BLOCK, typename OffT, bool CG = false>
+__device__ __forceinline__ void medium_tile(u32* keys, uint2 tl, const u64* __restrict__ fo,
+                                            const u32* __restrict__ head, const Desc<OffT>* __restrict__ vdesc,
+                                            const u32* __restrict__ headp, u32 seg, u64* __restrict__ cnt,
+                                            u64& local_total, u32& dup) {
+    using L = MediumLayout<BLOCK>;
+    constexpr int U = 4;  // medium owners' streamed lists are shorter than 256 entries
+    const int lane = threadIdx.x & 31;
+    u32* hitc = keys + L::TS;
+    u32* filt = hitc + L::TS / 2;
+    u32* wbuf = filt + L::FW;
+    const u32 lt_mask = (1u << lane) - 1;
+    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
+    const u64 x = tl.x;
+    const Desc<OffT> dxd = ld_desc<CG>(vdesc + x);
+    const u32 dx = dxd.d;
+    const u64 fx1 = ld_in<CG>(fo + x + 1);
+    const u64 a = ld_in<CG>(fo + x) + (u64)tl.y * seg;
+    const u64 b = a + seg < fx1 ? a + seg : fx1;
+    u32 lg, fl;
+    chunk_sizes(dx, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FW * 32)), &lg, &fl);
+    const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
+    for (u32 i = lane; i < size; i += 32) keys[i] = EMPTY_KEY;
+    for (u32 i = lane; i < size / 2; i += 32) hitc[i] = 0;
+    for (u32 i = lane; i < fwords; i += 32) filt[i] = 0;
+    __syncwarp();
+    for (u32 q = lane; q < dx; q += 32) {
+        const u32 w = ld_in<CG>(headp + list_start(dxd) + q);
+        if (!bucket_insert(keys, lg, w)) dup = 1;
+        const u32 h = filter_bit(w, fl);
+        atomicOr(&filt[h >> 5], 1u << (h & 31u));
+    }
+    __syncwarp();
+    u32 T = 0;
+    for (u64 e0 = a; e0 < b; e0 += 32) {
+        const u64 e = e0 + lane;
+        u32 y = 0;
+        Desc<OffT> vy;
+        vy.start = 0;
+        vy.d = 0;
+        bool longl = false;
+        if (e < b) {
+            y = ld_in<CG>(head + e);
+            vy = ld_desc<CG>(vdesc + y);
+            const u32 dy = vy.d;
+            if (dy > 0 && key_less(dy, y, dx, x)) {
+                if (dy <= (u32)LONG_LIST) {
+                    const u32 hits = lane_stream_short<OffT, CG>(headp4, vy, keys, hitc, lg, filt, fl);
+                    if (hits) {
+                        atomicAdd(&cnt[y], (u64)hits);
+                        T += hits;
+                    }
+                } else {
+                    longl = true;
+                }
+            }
+        }
+        u32 ball = __ballot_sync(0xFFFFFFFFu, longl);
+        while (ball) {  // the warp streams this chunk's long lists one at a time
+            const int src = __ffs(ball) - 1;
+            ball &= ball - 1;
+            const u32 yy = __shfl_sync(0xFFFFFFFFu, y, src);
+            const u64 ys = (u64)__shfl_sync(0xFFFFFFFFu, (unsigned long long)list_start(vy), src);
+            const u32 yd = __shfl_sync(0xFFFFFFFFu, vy.d, src);
+            u32 hits = warp_stream_list<U, CG>(headp + ys, yd, keys, hitc, lg, filt, fl, wbuf, lane, lt_mask);
+            hits = __reduce_add_sync(0xFFFFFFFFu, hits);
+            if (lane == 0 && hits) {
+                atomicAdd(&cnt[yy], (u64)hits);
+                T += hits;
+            }
+        }
+    }
+    __syncwarp();
+    for (u32 i = lane; i < size; i += 32) {
+        const u32 h = read16(hitc, i);
+        if (h) atomicAdd(&cnt[keys[i]], (u64)h);
+    }
+    const u32 wt = __reduce_add_sync(0xFFFFFFFFu, T);
+    if (lane == 0 && wt) {
+        atomicAdd(&cnt[x], (u64)wt);
+        local_total += wt;
+    }
+    __syncwarp();
+}
+
 template <int BLOCK, typename OffT>
 __global__ void __launch_bounds__(BLOCK)
     k_count_medium(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
@@ -814,18 +786,13 @@ __global__ void __launch_bounds__(BLOCK)
                    const uint2* __restrict__ mtiles, u32 seg, u64* __restrict__ cnt,
                    u64* __restrict__ partials, Control* ctl) {
     using L = MediumLayout<BLOCK>;
-    constexpr int U = 4;  // medium owners' streamed lists are shorter than 256 entries
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ u64 s_red[L::NW];
+    (void)n;
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     u32* keys = reinterpret_cast<u32*>(smem) + warp * L::PER_WARP;
-    u32* hitc = keys + L::TS;
-    u32* filt = hitc + L::TS / 2;
-    u32* wbuf = filt + L::FW;
-    const u32 lt_mask = (1u << lane) - 1;
     const u64 ntiles = *(volatile unsigned long long*)&ctl->medium_tiles;
-    const uint4* headp4 = reinterpret_cast<const uint4*>(headp);
     u64 local_total = 0;
     u32 dup = 0;
     while (true) {
@@ -833,95 +800,26 @@ __global__ void __launch_bounds__(BLOCK)
         if (lane == 0) t = atomicAdd(&ctl->medium_next, 1ull);
         t = __shfl_sync(0xFFFFFFFFu, t, 0);
         if (t >= ntiles) break;
-        const uint2 tl = mtiles[t];
-        const u64 x = tl.x;
-        const Desc<OffT> dxd = load_desc(vdesc + x);
-        const u32 dx = dxd.d;
-        const u64 fx1 = fo[x + 1];
-        const u64 a = fo[x] + (u64)tl.y * seg;
-        const u64 b = a + seg < fx1 ? a + seg : fx1;
-        u32 lg, fl;
-        chunk_sizes(dx, 31 - __clz((u32)L::TS), 31 - __clz((u32)(L::FW * 32)), &lg, &fl);
-        const u32 size = 1u << lg, fwords = (1u << fl) >> 5;
-        for (u32 i = lane; i < size; i += 32) keys[i] = EMPTY_KEY;
-        for (u32 i = lane; i < size / 2; i += 32) hitc[i] = 0;
-        for (u32 i = lane; i < fwords; i += 32) filt[i] = 0;
-        __syncwarp();
-        for (u32 q = lane; q < dx; q += 32) {
-            const u32 w = __ldg(headp + list_start(dxd) + q);
-            if (!bucket_insert(keys, lg, w)) dup = 1;
-            const u32 h = filter_bit(w, fl);
-            atomicOr(&filt[h >> 5], 1u << (h & 31u));
-        }
-        __syncwarp();
-        u32 T = 0;
-        for (u64 e0 = a; e0 < b; e0 += 32) {
-            const u64 e = e0 + lane;
-            u32 y = 0;
-            Desc<OffT> vy;
-            vy.start = 0;
-            vy.d = 0;
-            bool longl = false;
-            if (e < b) {
-                y = __ldg(head + e);
-                vy = load_desc(vdesc + y);
-                const u32 dy = vy.d;
-                if (dy > 0 && key_less(dy, y, dx, x)) {
-                    if (dy <= (u32)LONG_LIST) {
-                        const u32 hits = lane_stream_short<OffT>(headp4, vy, keys, hitc, lg, filt, fl);
-                        if (hits) {
-                            atomicAdd(&cnt[y], (u64)hits);
-                            T += hits;
-                        }
-                    } else {
-                        longl = true;
-                    }
-                }
-            }
-            u32 ball = __ballot_sync(0xFFFFFFFFu, longl);
-            while (ball) {  // the warp streams this chunk's long lists one at a time
-                const int src = __ffs(ball) - 1;
-                ball &= ball - 1;
-                const u32 yy = __shfl_sync(0xFFFFFFFFu, y, src);
-                const u64 ys = (u64)__shfl_sync(0xFFFFFFFFu, (unsigned long long)list_start(vy), src);
-                const u32 yd = __shfl_sync(0xFFFFFFFFu, vy.d, src);
-                u32 hits = warp_stream_list<U>(headp + ys, yd, keys, hitc, lg, filt, fl, wbuf, lane, lt_mask);
-                hits = __reduce_add_sync(0xFFFFFFFFu, hits);
-                if (lane == 0 && hits) {
-                    atomicAdd(&cnt[yy], (u64)hits);
-                    T += hits;
-                }
-            }
-        }
-        __syncwarp();
-        for (u32 i = lane; i < size; i += 32) {
-            const u32 h = read16(hitc, i);
-            if (h) atomicAdd(&cnt[keys[i]], (u64)h);
-        }
-        const u32 wt = __reduce_add_sync(0xFFFFFFFFu, T);
-        if (lane == 0 && wt) {
-            atomicAdd(&cnt[x], (u64)wt);
-            local_total += wt;
-        }
-        __syncwarp();
+        medium_tile<BLOCK, OffT>(keys, mtiles[t], fo, head, vdesc, headp, seg, cnt, local_total, dup);
     }
     if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
     const u64 bt = block_sum_u64<BLOCK>(local_total, s_red);
     if (threadIdx.x == 0) partials[blockIdx.x] = bt;
 }
 
-// Sum of the per-block partial totals (a u64 tree reduction in one block).  After a device
-// error (invalid input, a bounded wait that ran out) the partials are incomplete or stale, so
-// the total is written as 0.
-__global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials, u32 np, u64* total,
-                                                const Control* ctl) {
+// Sum of the per-block partial totals (a u64 tree reduction in one block), without the slots
+// [skip0, skip1) of blocks that were not launched.  After a device error (invalid input, a
+// bounded wait that ran out) the partials are incomplete or stale, so the total is written as 0.
+__global__ void __launch_bounds__(1024) k_final(const u64* __restrict__ partials, u32 np, u32 skip0, u32 skip1,
+                                                u64* total, const Control* ctl) {
     __shared__ u64 s_red[32];
     if (*(volatile const u32*)&ctl->err & DEV_ERR_MASK) {
         if (threadIdx.x == 0) *total = 0;
         return;
     }
     u64 s = 0;
-    for (u32 i = threadIdx.x; i < np; i += 1024) s += partials[i];
+    for (u32 i = threadIdx.x; i < np; i += 1024)
+        if (i < skip0 || i >= skip1) s += partials[i];
     const u64 t = block_sum_u64<1024>(s, s_red);
     if (threadIdx.x == 0) *total = t;
 }
@@ -996,11 +894,218 @@ __global__ void k_stats(const u64* __restrict__ fo, const u32* __restrict__ head
     }
 }
 
+// ---- the serving engine ----------------------------------------------------------------
+
+constexpr int ENGINE_SD = SMALL_D;  // the small-owner layout for any small_outdegree bound
+using EngineSmallL = SmallWarpLayout<ENGINE_SD, u32>;
+using EngineMediumL = MediumLayout<ENGINE_BLOCK>;
+using EngineLargeL = LargeLayout<ENGINE_BLOCK, LARGE_CAP, u32>;
+constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
+constexpr size_t ENGINE_SMEM =
+    cmax(cmax(EngineSmallL::bytes(ENGINE_BLOCK / 32), EngineMediumL::bytes), EngineLargeL::bytes);
+static_assert(SMALL_BLOCK == ENGINE_BLOCK && MEDIUM_BLOCK == ENGINE_BLOCK && LARGE_BLOCK == ENGINE_BLOCK,
+              "the engine runs every kind of unit with one block shape");
+
+// The claim cursor of a job holds the publication's tag (low 24 bits of its sequence number) in
+// its top 24 bits and the next unit in its low 40 bits.  Units are claimed by compare-and-swap
+// against a cursor whose tag matches the sequence number read before and after it, so a block
+// can never take a unit of a later publication of the same slot, nor read a half-written record.
+constexpr int ENGINE_TAG_SHIFT = 40;
+constexpr unsigned long long ENGINE_COUNT_MASK = (1ull << ENGINE_TAG_SHIFT) - 1;
+__device__ __forceinline__ unsigned long long engine_tag(unsigned long long seq) { return seq & 0xFFFFFFull; }
+
+__global__ void k_publish(EngineJob* job, unsigned long long seq, const u64* fo, const u32* head, u64 n,
+                          const void* vdesc, const u32* headp, const uint2* mtiles, const uint2* ltiles, u64* cnt,
+                          Control* ctl, u32 small_d, u32 seg, unsigned long long* done_word) {
+    if (threadIdx.x != 0) return;
+    volatile EngineJob* vj = job;
+    vj->seq = 0;  // unpublished while the record changes
+    __threadfence();
+    const bool bad = (*(volatile u32*)&ctl->err & DEV_ERR_MASK) != 0;
+    const unsigned long long nbatch = (n + 31) / 32;
+    const unsigned long long us = bad ? 0 : (nbatch + ENGINE_UNIT_ITEMS - 1) / ENGINE_UNIT_ITEMS;
+    const unsigned long long um =
+        bad ? 0 : (*(volatile unsigned long long*)&ctl->medium_tiles + ENGINE_UNIT_ITEMS - 1) / ENGINE_UNIT_ITEMS;
+    const unsigned long long ul = bad ? 0 : *(volatile unsigned long long*)&ctl->large_tiles;
+    if (us + um + ul == 0) {  // nothing for the engine: done at once
+        __threadfence_system();
+        *(volatile unsigned long long*)done_word = seq;
+        return;
+    }
+    vj->fo = fo;
+    vj->head = head;
+    vj->n = n;
+    vj->vdesc = vdesc;
+    vj->headp = headp;
+    vj->mtiles = mtiles;
+    vj->ltiles = ltiles;
+    vj->cnt = cnt;
+    vj->ctl = ctl;
+    vj->small_d = small_d;
+    vj->seg = seg;
+    vj->units_small = us;
+    vj->units_medium = um;
+    vj->units = us + um + ul;
+    vj->done = 0;
+    __threadfence();
+    vj->next = engine_tag(seq) << ENGINE_TAG_SHIFT;
+    __threadfence();
+    vj->seq = seq;
+}
+
+__global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words,
+                                                         const unsigned* stop, u32 idle_polls) {
+    constexpr int BLOCK = ENGINE_BLOCK;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_job;
+    __shared__ unsigned long long s_unit;
+    __shared__ EngineJob s_jb;  // the claimed job's record, read at L2 by thread 0
+    __shared__ u32 s_jb_slot;
+    __shared__ unsigned s_stop;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    (void)lane;
+    // the large-owner tiles' bulk-copy barrier lives in the large layout's scalar area
+    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem + EngineLargeL::off_bar);
+    if (threadIdx.x == 0) {
+        mbar_init(s_bar, 1);
+        s_jb.seq = 0;
+        s_jb_slot = 0xFFFFFFFFu;
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    u32 phase = 0;
+    bool inflight = false;
+    u32 idle = 0, start = blockIdx.x % (njobs ? njobs : 1);
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_job = -1;
+            s_stop = *(volatile const unsigned*)stop;
+            for (u32 k = 0; k < njobs && s_job < 0; ++k) {
+                const u32 j = (start + k) % njobs;
+                volatile EngineJob* vj = jobs + j;
+                for (int attempt = 0; attempt < 4; ++attempt) {
+                    const unsigned long long s1 = vj->seq;
+                    if (s1 == 0) break;
+                    __threadfence();
+                    const unsigned long long cur = vj->next;
+                    const unsigned long long units = vj->units;
+                    __threadfence();
+                    if (vj->seq != s1 || (cur >> ENGINE_TAG_SHIFT) != engine_tag(s1)) break;
+                    if ((cur & ENGINE_COUNT_MASK) >= units) break;
+                    if (atomicCAS(const_cast<unsigned long long*>(&vj->next), cur, cur + 1) != cur) continue;
+                    // unit (cur & mask) of publication s1: its record stays as it is until the job
+                    // is done, which needs this unit
+                    s_job = (int)j;
+                    s_unit = cur & ENGINE_COUNT_MASK;
+                    start = j;
+                    if (s_jb.seq == s1 && s_jb_slot == j) break;  // this block holds the record already
+                    s_jb_slot = j;
+                    s_jb.fo = vj->fo;
+                    s_jb.head = vj->head;
+                    s_jb.n = vj->n;
+                    s_jb.vdesc = vj->vdesc;
+                    s_jb.headp = vj->headp;
+                    s_jb.mtiles = vj->mtiles;
+                    s_jb.ltiles = vj->ltiles;
+                    s_jb.cnt = vj->cnt;
+                    s_jb.ctl = vj->ctl;
+                    s_jb.small_d = vj->small_d;
+                    s_jb.seg = vj->seg;
+                    s_jb.units_small = vj->units_small;
+                    s_jb.units_medium = vj->units_medium;
+                    s_jb.units = units;
+                    s_jb.seq = s1;
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        const int j = s_job;
+        if (j < 0) {
+            if (++idle > idle_polls || s_stop) break;  // the same decision in every thread
+            __nanosleep(2000);
+            __syncthreads();  // every thread has read s_job before thread 0 writes it again
+            continue;
+        }
+        idle = 0;
+        const EngineJob* jb = &s_jb;
+        const unsigned long long u = s_unit;
+        Control* ctl = jb->ctl;
+        const auto* vd = reinterpret_cast<const Desc<u32>*>(jb->vdesc);
+        u64 unused_total = 0;
+        u32 dup = 0;
+        bool timed_out = false;
+        if (u < jb->units_small) {
+            const u64 nb = (jb->n + 31) / 32;
+            for (u32 r = 0; r < ENGINE_REPS; ++r) {
+                const u64 bi = (u * (ENGINE_BLOCK / 32) + warp) * ENGINE_REPS + r;
+                if (bi < nb)
+                    small_batch<ENGINE_SD, u32, true>(reinterpret_cast<u32*>(smem) + warp * EngineSmallL::PER_WARP, bi,
+                                                      jb->fo, jb->head, jb->n, vd, jb->headp, jb->small_d, jb->cnt,
+                                                      unused_total, dup);
+            }
+        } else if (u < jb->units_small + jb->units_medium) {
+            const u64 nt = *(volatile unsigned long long*)&ctl->medium_tiles;
+            for (u32 r = 0; r < ENGINE_REPS; ++r) {
+                const u64 t = ((u - jb->units_small) * (ENGINE_BLOCK / 32) + warp) * ENGINE_REPS + r;
+                if (t < nt)
+                    medium_tile<BLOCK, u32, true>(reinterpret_cast<u32*>(smem) + warp * EngineMediumL::PER_WARP,
+                                                  __ldcg(jb->mtiles + t), jb->fo, jb->head, vd, jb->headp, jb->seg,
+                                                  jb->cnt, unused_total, dup);
+            }
+        } else {
+            const u64 t = u - jb->units_small - jb->units_medium;
+            timed_out = large_tile<BLOCK, LARGE_CAP, u32, true>(smem, __ldcg(jb->ltiles + t), jb->fo, jb->head, jb->n, vd,
+                                                                jb->headp,
+                                                          jb->seg, jb->cnt, COPY_WAIT_POLLS, phase, inflight,
+                                                          unused_total, dup);
+        }
+        if (dup) atomicOr(&ctl->err, DEV_ERR_DUPLICATE);
+        if (timed_out && threadIdx.x == 0)
+            atomicOr(&ctl->err, DEV_ERR_TIMEOUT | (inflight ? DEV_ERR_COPY_INFLIGHT : 0u));
+        __syncthreads();  // the unit's counts are all issued
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned long long d = atomicAdd(&jobs[j].done, 1ull) + 1;
+            if (d == jb->units) {
+                *(volatile unsigned long long*)&jobs[j].seq = 0;
+                __threadfence_system();
+                *(volatile unsigned long long*)(done_words + j) = jb->seq;
+            }
+        }
+        // a copy that may still be landing in shared memory: this block stops taking units
+        if (inflight) break;
+    }
+}
+
+void launch_publish(EngineJob* job, unsigned long long seq, const u64* fo, const u32* head, u64 n,
+                    const void* vdesc, const u32* headp, const uint2* mtiles, const uint2* ltiles, u64* cnt,
+                    Control* ctl, u32 small_d, u32 seg, unsigned long long* done_word, cudaStream_t st) {
+    k_publish<<<1, 32, 0, st>>>(job, seq, fo, head, n, vdesc, headp, mtiles, ltiles, cnt, ctl, small_d, seg, done_word);
+}
+
+size_t engine_smem_bytes() { return ENGINE_SMEM; }
+
+int engine_grid(int num_sms) {
+    static int occ = -1;
+    if (occ < 0) {
+        cudaFuncSetAttribute(k_engine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENGINE_SMEM);
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_engine, ENGINE_BLOCK, ENGINE_SMEM);
+        occ = o > 0 ? o : 1;
+    }
+    // leave room on every SM for the preparation kernels of the batches being published
+    return num_sms * (occ > 1 ? occ - 1 : 1);
+}
+
+void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, const unsigned* stop, u32 idle_polls,
+                   int grid, cudaStream_t st) {
+    k_engine<<<grid, ENGINE_BLOCK, ENGINE_SMEM, st>>>(jobs, njobs, done_words, stop, idle_polls);
+}
+
 // ---- launchers ------------------------------------------------------------------------
 
 namespace {
-template <int SD, typename OffT>
-using SmallL = SmallLayout<SMALL_BLOCK, SMALL_IPT, SD, OffT>;
 template <typename OffT>
 using LargeL = LargeLayout<LARGE_BLOCK, LARGE_CAP, OffT>;
 using MediumL = MediumLayout<MEDIUM_BLOCK>;
@@ -1009,20 +1114,11 @@ template <int SD, typename OffT>
 int occupancy_small() {
     static int occ = -1;
     if (occ < 0) {
-        auto kern = k_count_small<SMALL_BLOCK, SMALL_IPT, SD, OffT>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmallL<SD, OffT>::bytes);
+        auto kern = k_count_small<SMALL_BLOCK, SD, OffT>;
+        const size_t bytes = SmallWarpLayout<SD, OffT>::bytes(SMALL_BLOCK / 32);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, SmallL<SD, OffT>::bytes);
-        occ = o > 0 ? o : 1;
-    }
-    return occ;
-}
-template <int SD, typename OffT>
-int occupancy_small_warp() {
-    static int occ = -1;
-    if (occ < 0) {
-        int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_count_small_warp<SMALL_BLOCK, SD, OffT>, SMALL_BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, SMALL_BLOCK, bytes);
         occ = o > 0 ? o : 1;
     }
     return occ;
@@ -1054,10 +1150,7 @@ int occupancy_large() {
 }  // namespace
 
 template <typename OffT>
-int count_grid_small(int num_sms, u32 small_d, bool warp) {
-    if (warp)
-        return num_sms * (small_d <= (u32)SMALL_D_LOW ? occupancy_small_warp<SMALL_D_LOW, OffT>()
-                                                      : occupancy_small_warp<SMALL_D, OffT>());
+int count_grid_small(int num_sms, u32 small_d) {
     return num_sms * (small_d <= (u32)SMALL_D_LOW ? occupancy_small<SMALL_D_LOW, OffT>()
                                                   : occupancy_small<SMALL_D, OffT>());
 }
@@ -1069,39 +1162,43 @@ template <typename OffT>
 int count_grid_large(int num_sms) {
     return num_sms * occupancy_large<OffT>();
 }
+// Blocks the small-owner kernel is launched with: enough for one vertex batch per warp, at most
+// its resident grid (a small graph does not start hundreds of warps that find no batch).
+int small_grid_launched(u64 n, int cap) {
+    const u64 need = ((n + 31) / 32 + SMALL_BLOCK / 32 - 1) / (SMALL_BLOCK / 32);
+    return (int)(need < 1 ? 1 : (need < (u64)cap ? need : (u64)cap));
+}
+
 template <typename OffT>
-int count_grid_auto(int num_sms, u32 small_d, bool warp) {
-    return count_grid_small<OffT>(num_sms, small_d, warp) + count_grid_medium<OffT>(num_sms) +
+int count_grid_auto(int num_sms, u32 small_d) {
+    return count_grid_small<OffT>(num_sms, small_d) + count_grid_medium<OffT>(num_sms) +
            count_grid_large<OffT>(num_sms);
 }
 
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
-                              u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
-                              cudaEvent_t after_small, cudaEvent_t after_large, u32 copy_wait_polls,
-                              bool small_warp) {
-    const int gs = count_grid_small<OffT>(num_sms, small_d, small_warp);
+                              const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg, u64* cnt, u64* partials,
+                              Control* ctl, int num_sms, cudaStream_t st, cudaEvent_t after_small,
+                              cudaEvent_t after_large, u32 copy_wait_polls) {
+    (void)nnz;
+    const int cap = count_grid_small<OffT>(num_sms, small_d);
+    const int gs = small_grid_launched(n, cap);
     const int gm = count_grid_medium<OffT>(num_sms);
     const int gl = count_grid_large<OffT>(num_sms);
     const auto* vd = reinterpret_cast<const Desc<OffT>*>(vdesc);
-    if (small_warp && small_d <= (u32)SMALL_D_LOW)
-        k_count_small_warp<SMALL_BLOCK, SMALL_D_LOW, OffT>
-            <<<gs, SMALL_BLOCK, 0, st>>>(fo, head, n, vd, headp, small_d, cnt, partials, ctl);
-    else if (small_warp)
-        k_count_small_warp<SMALL_BLOCK, SMALL_D, OffT>
-            <<<gs, SMALL_BLOCK, 0, st>>>(fo, head, n, vd, headp, small_d, cnt, partials, ctl);
-    else if (small_d <= (u32)SMALL_D_LOW)
-        k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D_LOW, OffT><<<gs, SMALL_BLOCK, SmallL<SMALL_D_LOW, OffT>::bytes, st>>>(
-            fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials, ctl);
+    if (small_d <= (u32)SMALL_D_LOW)
+        k_count_small<SMALL_BLOCK, SMALL_D_LOW, OffT>
+            <<<gs, SMALL_BLOCK, SmallWarpLayout<SMALL_D_LOW, OffT>::bytes(SMALL_BLOCK / 32), st>>>(
+                fo, head, n, vd, headp, small_d, cnt, partials, ctl);
     else
-        k_count_small<SMALL_BLOCK, SMALL_IPT, SMALL_D, OffT><<<gs, SMALL_BLOCK, SmallL<SMALL_D, OffT>::bytes, st>>>(
-            fo, head, n, nnz, vd, headp, tile_i0, small_d, cnt, partials, ctl);
+        k_count_small<SMALL_BLOCK, SMALL_D, OffT>
+            <<<gs, SMALL_BLOCK, SmallWarpLayout<SMALL_D, OffT>::bytes(SMALL_BLOCK / 32), st>>>(
+                fo, head, n, vd, headp, small_d, cnt, partials, ctl);
     if (after_small) cudaEventRecord(after_small, st);
     k_count_medium<MEDIUM_BLOCK, OffT>
-        <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, seg, cnt, partials + gs, ctl);
+        <<<gm, MEDIUM_BLOCK, MediumL::bytes, st>>>(fo, head, n, vd, headp, mtiles, seg, cnt, partials + cap, ctl);
     k_count_large<LARGE_BLOCK, LARGE_CAP, OffT>
-        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, seg, cnt, partials + gs + gm,
+        <<<gl, LARGE_BLOCK, LargeL<OffT>::bytes, st>>>(fo, head, n, vd, headp, ltiles, seg, cnt, partials + cap + gm,
                                                        ctl, copy_wait_polls);
     if (after_large) cudaEventRecord(after_large, st);
     return cudaGetLastError();
@@ -1115,7 +1212,15 @@ void launch_graph_totals(const u64* cnt, const u64* graph_first, u64 num_graphs,
 }
 
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st) {
-    k_final<<<1, 1024, 0, st>>>(partials, np, total, ctl);
+    k_final<<<1, 1024, 0, st>>>(partials, np, 0, 0, total, ctl);
+}
+
+template <typename OffT>
+void launch_final_auto(const u64* partials, u64 n, u32 small_d, int num_sms, u64* total, Control* ctl,
+                       cudaStream_t st) {
+    const int cap = count_grid_small<OffT>(num_sms, small_d);
+    k_final<<<1, 1024, 0, st>>>(partials, (u32)count_grid_auto<OffT>(num_sms, small_d), (u32)small_grid_launched(n, cap),
+                                (u32)cap, total, ctl);
 }
 
 template <typename OffT>
@@ -1126,22 +1231,22 @@ void launch_stats(const u64* fo, const u32* head, u64 n, const void* vdesc, cons
                                                medium_d, ctl);
 }
 
-template int count_grid_small<u32>(int, u32, bool);
-template int count_grid_small<u64>(int, u32, bool);
+template void launch_final_auto<u32>(const u64*, u64, u32, int, u64*, Control*, cudaStream_t);
+template void launch_final_auto<u64>(const u64*, u64, u32, int, u64*, Control*, cudaStream_t);
+template int count_grid_small<u32>(int, u32);
+template int count_grid_small<u64>(int, u32);
 template int count_grid_large<u32>(int);
 template int count_grid_large<u64>(int);
 template int count_grid_medium<u32>(int);
 template int count_grid_medium<u64>(int);
-template int count_grid_auto<u32>(int, u32, bool);
-template int count_grid_auto<u64>(int, u32, bool);
-template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const uint2*, u32, u32,
-                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t, u32,
-                                            bool);
-template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const u32*,
-                                            const uint2*, const uint2*, u32, u32,
-                                            u64*, u64*, Control*, int, cudaStream_t, cudaEvent_t, cudaEvent_t, u32,
-                                            bool);
+template int count_grid_auto<u32>(int, u32);
+template int count_grid_auto<u64>(int, u32);
+template cudaError_t launch_count_auto<u32>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+                                            const uint2*, u32, u32, u64*, u64*, Control*, int, cudaStream_t,
+                                            cudaEvent_t, cudaEvent_t, u32);
+template cudaError_t launch_count_auto<u64>(const u64*, const u32*, u64, u64, const void*, const u32*, const uint2*,
+                                            const uint2*, u32, u32, u64*, u64*, Control*, int, cudaStream_t,
+                                            cudaEvent_t, cudaEvent_t, u32);
 template void launch_stats<u32>(const u64*, const u32*, u64, const void*, const u32*, u32, Control*, int,
                                 cudaStream_t);
 template void launch_stats<u64>(const u64*, const u32*, u64, const void*, const u32*, u32, Control*, int,

@@ -27,11 +27,23 @@ struct Options {
     bool force_wide = false;
     uint32_t copy_wait_polls = 0;    // polls of the first wait for an owner chunk's bulk copy (0 = default)
     uint32_t tile_order = 0;         // 0: by streamed vertex / owner degree; KTRI_TILE_ORDER_COST: by tile work
-    bool small_warp = false;         // small owners: warp-per-owner kernel instead of merge-path tiles
 };
 
-// The device a context was created on.
+// The device a context was created on, and its SM count.
 int ctx_device(const ktri_ctx* ctx);
+int ctx_num_sms(const ktri_ctx* ctx);
+
+struct Control;
+struct EngineJob;
+// Serving engine: enqueue the preparation of a packed batch (orientation, descriptors, owner
+// tiles) on ctx's workspace and `stream`, then publish its counting phase as job `job` with
+// sequence number seq; done_word (device address of host-mapped memory) receives seq when the
+// engine has counted it.  Per-vertex counts go to d_per_vertex; *ctl_out is the batch's control
+// block (for the graph totals after completion).  Batches that need 64-bit descriptors return
+// KTRI_ERR_UNSUPPORTED (count them with ktri_count_batch_device).
+int engine_prepare_batch(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_head, uint64_t n_total,
+                         uint64_t nnz_total, uint64_t* d_per_vertex, void* stream, EngineJob* job,
+                         unsigned long long seq, unsigned long long* done_word, Control** ctl_out);
 
 // Device-side error bits written by the kernels (one u32 word in the control block).
 enum : uint32_t {

@@ -15,10 +15,9 @@ using u64 = unsigned long long;
 constexpr int ORIENT_BLOCK = 128;
 constexpr int ORIENT_IPT = 6;
 constexpr int SMALL_BLOCK = 256;
-constexpr int SMALL_IPT = 3;
-constexpr int SMALL_D = 48;          // largest out-degree bound of the tile kernel's owners
-constexpr int SMALL_D_LOW = 32;      // bounds up to this run the tile kernel's instantiation for 32,
-                                     // the others the one for SMALL_D (more table and bin space)
+constexpr int SMALL_D = 48;          // largest out-degree bound of the small-owner kernel's owners
+constexpr int SMALL_D_LOW = 32;      // bounds up to this run the small-owner kernel's instantiation for
+                                     // 32, the others the one for SMALL_D (more table and bin space)
 constexpr int MEDIUM_D = 256;        // out-degree bound of the warp-per-tile kernel's owners
 constexpr int MEDIUM_BLOCK = 256;
 constexpr int LARGE_BLOCK = 256;
@@ -27,16 +26,15 @@ constexpr u32 LARGE_SEG = 1024;      // most adjacency slots per (owner, segment
 constexpr u32 MIN_SEG = 64;          // fewest adjacency slots per (owner, segment) tile
 constexpr int LONG_LIST = 16;        // lists longer than this are streamed by a whole warp
 constexpr u32 COPY_WAIT_POLLS = 1u << 22;  // polls of a bounded wait for a bulk copy into shared memory
-constexpr u32 SMALL_WARP_DEG = 256;  // the warp-per-owner small kernel takes owners up to this degree; owners
-                                     // of larger degree (and small out-degree) go to the medium kernel's tiles
+constexpr u32 SMALL_WARP_DEG = 256;  // the small-owner kernel takes owners up to this degree; owners of
+                                     // larger degree (and small out-degree) go to the medium kernel's tiles
 
 inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
 // Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
-// the vertex where diagonal k * TILE_BASE crosses the path.  The counting tiles are one base
-// tile, the orientation tiles ORIENT_PER_BASE of them.
-constexpr u64 TILE_BASE = (u64)SMALL_BLOCK * SMALL_IPT;
-constexpr u64 ORIENT_PER_BASE = (u64)ORIENT_BLOCK * ORIENT_IPT / TILE_BASE;
-static_assert(ORIENT_PER_BASE * TILE_BASE == (u64)ORIENT_BLOCK * ORIENT_IPT, "orientation tile = whole base tiles");
+// the vertex where diagonal k * TILE_BASE crosses the path.  An orientation tile is one base
+// tile.
+constexpr u64 TILE_BASE = (u64)ORIENT_BLOCK * ORIENT_IPT;
+constexpr u64 ORIENT_PER_BASE = 1;
 inline u64 base_tiles(u64 n, u64 nnz) { return (n + nnz + TILE_BASE - 1) / TILE_BASE; }
 // Owners above small_d hold more than small_d adjacency entries each, and owners routed to the
 // tiles for their degree more than SMALL_WARP_DEG; every owner has at most deg / seg + 1 tiles.
@@ -81,7 +79,7 @@ void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, 
 // Orientation over merge-path tiles [tile_begin, tile_end) of ORIENT_TILE items (all by
 // default).  Tile t reads adjacency slots below (t + 1) * ORIENT_TILE + 1 only, so it may run
 // as soon as that prefix of head is on the device.
-constexpr u64 ORIENT_TILE = (u64)ORIENT_BLOCK * ORIENT_IPT;
+constexpr u64 ORIENT_TILE = TILE_BASE;
 u64 orient_tiles(u64 n, u64 nnz);
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
                    u32* dplus, u32* spanning, Control* ctl, cudaStream_t st, u64 tile_begin = 0,
@@ -89,7 +87,7 @@ void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* de
 // Owner tiles: medium owners' tiles are written to mtiles, large owners' to ltiles (each
 // array holds large_tile_capacity entries).
 // small_deg_max: owners up to small_d whose degree exceeds it get medium tiles too (the
-// warp-per-owner small kernel's bound; ~0u with the tile kernel, which takes any degree).
+// small-owner kernel's bound, SMALL_WARP_DEG).
 template <typename OffT>
 void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mtiles, uint2* ltiles, u32 small_d,
                  u32 medium_d, u32 seg, u32 small_deg_max, Control* ctl, int num_sms, cudaStream_t st);
@@ -108,20 +106,65 @@ void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n,
 
 // Owner-side hash counting (KTRI_METHOD_AUTO).  partials needs small_grid + large_grid entries.
 template <typename OffT>
-int count_grid_small(int num_sms, u32 small_d, bool warp);
+int count_grid_small(int num_sms, u32 small_d);
 template <typename OffT>
 int count_grid_medium(int num_sms);
 template <typename OffT>
 int count_grid_large(int num_sms);
 template <typename OffT>
-int count_grid_auto(int num_sms, u32 small_d, bool warp);  // small + medium + large, for this small-owner bound
+int count_grid_auto(int num_sms, u32 small_d);  // small + medium + large, for this small-owner bound
 template <typename OffT>
 cudaError_t launch_count_auto(const u64* fo, const u32* head, u64 n, u64 nnz, const void* vdesc, const u32* headp,
-                              const u32* tile_i0, const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg,
-                              u64* cnt, u64* partials, Control* ctl, int num_sms, cudaStream_t st,
-                              cudaEvent_t after_small, cudaEvent_t after_large,
-                              u32 copy_wait_polls = COPY_WAIT_POLLS, bool small_warp = false);
+                              const uint2* mtiles, const uint2* ltiles, u32 small_d, u32 seg, u64* cnt, u64* partials,
+                              Control* ctl, int num_sms, cudaStream_t st, cudaEvent_t after_small,
+                              cudaEvent_t after_large, u32 copy_wait_polls = COPY_WAIT_POLLS);
 void launch_final(const u64* partials, u32 np, u64* total, Control* ctl, cudaStream_t st);
+// The total of an AUTO count (the small-owner kernel's grid depends on n).
+int small_grid_launched(u64 n, int cap);
+template <typename OffT>
+void launch_final_auto(const u64* partials, u64 n, u32 small_d, int num_sms, u64* total, Control* ctl,
+                       cudaStream_t st);
+
+// ---- the serving engine ------------------------------------------------------------------
+// A prepared batch (orientation, descriptors and owner tiles done on its slot's stream) is
+// published as a job; one persistent engine kernel per server drains the jobs' work units while
+// the host keeps publishing: ENGINE_UNIT_ITEMS vertex batches of 32 (small owners, a run of
+// ENGINE_REPS per warp), as many medium tiles (likewise) or one large tile (the whole block) per
+// unit.  The block that finishes a
+// job's last unit writes the job's sequence number into host-mapped memory.
+struct EngineJob {
+    const u64* fo;
+    const u32* head;
+    u64 n;
+    const void* vdesc;  // Desc<u32>: jobs use 32-bit descriptors
+    const u32* headp;
+    const uint2* mtiles;
+    const uint2* ltiles;
+    u64* cnt;
+    Control* ctl;
+    u32 small_d, seg;
+    unsigned long long units_small, units_medium, units;  // the rest are large tiles
+    unsigned long long next;  // claim cursor
+    unsigned long long done;  // finished units
+    unsigned long long seq;   // nonzero while published (written last)
+    unsigned long long pad[3];
+};
+constexpr int ENGINE_BLOCK = 256;
+constexpr u32 ENGINE_REPS = 4;  // vertex batches or medium tiles per warp and unit
+constexpr u32 ENGINE_UNIT_ITEMS = ENGINE_BLOCK / 32 * ENGINE_REPS;  // vertex batches or medium tiles per unit
+// Publish a prepared batch as job slot `job` with sequence number seq (on the batch's stream,
+// after its preparation).  A batch with nothing to count, or with invalid input, is marked done
+// at once: done_word (host-mapped) receives seq.
+void launch_publish(EngineJob* job, unsigned long long seq, const u64* fo, const u32* head, u64 n,
+                    const void* vdesc, const u32* headp, const uint2* mtiles, const uint2* ltiles, u64* cnt,
+                    Control* ctl, u32 small_d, u32 seg, unsigned long long* done_word, cudaStream_t st);
+// The engine: blocks drain published jobs and leave after idle_polls empty scans (about 2 us
+// each) or when *stop is nonzero.  done_words[j] (host-mapped) receives job j's sequence number
+// when its last unit is done.
+int engine_grid(int num_sms);
+size_t engine_smem_bytes();
+void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, const unsigned* stop, u32 idle_polls,
+                   int grid, cudaStream_t st);
 
 // u64 ids (the binary file format) -> u32 ids; ids above 2^32 - 1 become 0xFFFFFFFF.
 void launch_narrow_ids(const u64* src, u64 count, u32* dst, int num_sms, cudaStream_t st);

@@ -27,6 +27,8 @@
 
 #include "ktri.h"
 #include "ktri_device.cuh"
+#include "ktri_internal.h"
+#include "ktri_kernels.h"
 
 using ktri::u32;
 using ktri::u64;
@@ -199,6 +201,12 @@ struct Slot {
     size_t off_fo = 0, off_head = 0, off_vf = 0, off_ef = 0, off_tot = 0, off_pv = 0, off_src = 0;
     size_t h_tot = 0, h_pv = 0;
     bool direct = false;  // this batch was gathered from host memory by the device
+    // engine mode: the batch's counting phase is job (slot index) with this sequence number; the
+    // slot waits for the engine while counting is set, then reads back
+    unsigned long long seq = 0;
+    bool counting = false;
+    ktri::Control* ctl = nullptr;
+    double t_published = 0;
 };
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
@@ -226,6 +234,18 @@ struct ktri_server {
     ktri_server_stats st{};
     int fatal = KTRI_OK;
     double alloc_s_acc = 0;  // seconds spent in grow() by the worker, moved into st.alloc_us under the lock
+    // the engine: one persistent counting kernel that drains the slots' published jobs
+    bool engine = false;
+    ktri::EngineJob* jobs = nullptr;         // device, one per slot
+    unsigned long long* done_host = nullptr;  // host-mapped completion words, one per slot
+    unsigned long long* done_dev = nullptr;   // their device address
+    unsigned* stop_dev = nullptr;             // device flag: 1 tells the engine to leave
+    cudaStream_t engine_stream = nullptr;
+    cudaEvent_t engine_done = nullptr;        // recorded after each engine launch
+    bool engine_launched = false;
+    unsigned long long seq_next = 1;
+    int engine_grid = 0;
+    uint64_t engine_launches = 0;
 };
 
 namespace {
@@ -394,6 +414,79 @@ SlotLayout slot_layout(u64 n, u64 nnz, u64 k, bool direct) {
 }
 
 // Pack the slot's requests and launch their count.  Called without the lock.
+// Engine scans without a published job before an engine launch leaves (about 2 us each).
+constexpr unsigned ENGINE_IDLE_POLLS = 100;
+
+size_t slot_index(const ktri_server* s, const Slot& sl) { return (size_t)(&sl - s->slots.data()); }
+
+// Launch the engine unless one is running.  A job published while the running engine was
+// already leaving is picked up by the next launch, which the worker loop makes as soon as it
+// sees the previous one done and a slot still waiting.
+int ensure_engine(ktri_server* s) {
+    if (s->engine_launched) {
+        const cudaError_t q = cudaEventQuery(s->engine_done);
+        if (q == cudaErrorNotReady) return KTRI_OK;
+        if (q != cudaSuccess) return KTRI_ERR_CUDA;
+    }
+    ktri::launch_engine(s->jobs, (u32)s->slots.size(), s->done_dev, s->stop_dev, ENGINE_IDLE_POLLS, s->engine_grid,
+                        s->engine_stream);
+    cudaEventRecord(s->engine_done, s->engine_stream);
+    s->engine_launched = true;
+    s->st.engine_launches++;
+    return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
+}
+
+// Tell a running engine to leave, wait for it, and free its resources (the worker has ended).
+void release_engine(ktri_server* s) {
+    if (s->engine_launched && s->stop_dev) {
+        cudaMemsetAsync(s->stop_dev, 0xFF, sizeof(unsigned), s->aux);
+        cudaStreamSynchronize(s->engine_stream);
+    }
+    if (s->engine_done) cudaEventDestroy(s->engine_done);
+    if (s->engine_stream) cudaStreamDestroy(s->engine_stream);
+    if (s->jobs) cudaFree(s->jobs);
+    if (s->stop_dev) cudaFree(s->stop_dev);
+    if (s->done_host) cudaFreeHost(s->done_host);
+    s->engine_done = nullptr;
+    s->engine_stream = nullptr;
+    s->jobs = nullptr;
+    s->stop_dev = nullptr;
+    s->done_host = nullptr;
+    s->engine_launched = false;
+}
+
+// Read-back of a counted batch on its slot's stream: totals, per-vertex counts (into pinned
+// staging, or straight into the callers' memory), then the slot's done event.
+int enqueue_readback(ktri_server* s, Slot& sl) {
+    (void)s;
+    char* d = static_cast<char*>(sl.dev);
+    char* h = static_cast<char*>(sl.host);
+    cudaStream_t st = sl.stream;
+    const u64 k = sl.reqs.size(), n = sl.n_total;
+    cudaMemcpyAsync(h + sl.h_tot, d + sl.off_tot, 8 * k, cudaMemcpyDeviceToHost, st);
+    if (sl.direct) {
+        const u64 warps = (n + 255) / 256;
+        const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
+        k_scatter_pv<<<blocks, 256, 0, st>>>(reinterpret_cast<const GraphSrc*>(d + sl.off_src),
+                                             reinterpret_cast<const u64*>(d + sl.off_vf), k, n,
+                                             reinterpret_cast<const u64*>(d + sl.off_pv));
+    } else {
+        cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
+    }
+    cudaEventRecord(sl.done, st);
+    return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
+}
+
+// The engine has counted this slot's batch: per-graph totals from the per-vertex counts, then
+// the read-back.
+int finish_engine_batch(ktri_server* s, Slot& sl) {
+    char* d = static_cast<char*>(sl.dev);
+    ktri::launch_graph_totals(reinterpret_cast<const u64*>(d + sl.off_pv), reinterpret_cast<const u64*>(d + sl.off_vf),
+                              sl.reqs.size(), sl.n_total, reinterpret_cast<u64*>(d + sl.off_tot), sl.ctl,
+                              ktri::ctx_num_sms(sl.ctx), sl.stream);
+    return enqueue_readback(s, sl);
+}
+
 int launch_batch(ktri_server* s, Slot& sl) {
     const u64 k = sl.reqs.size();
     u64 n = 0, nnz = 0;
@@ -495,6 +588,21 @@ int launch_batch(ktri_server* s, Slot& sl) {
         k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k, n, nnz);
     }
     if (cudaGetLastError() != cudaSuccess) return KTRI_ERR_CUDA;
+    if (s->engine && n > 0) {
+        // prepare on this slot and publish to the engine; the read-back follows its completion
+        const size_t j = slot_index(s, sl);
+        sl.seq = s->seq_next++;
+        rc = ktri::engine_prepare_batch(sl.ctx, reinterpret_cast<const uint64_t*>(dfo), dhead, n, nnz,
+                                        reinterpret_cast<uint64_t*>(d + sl.off_pv), st, s->jobs + j, sl.seq,
+                                        s->done_dev + j, &sl.ctl);
+        if (rc == KTRI_OK) {
+            sl.counting = true;
+            sl.t_published = now_s();
+            return ensure_engine(s);
+        }
+        if (rc != KTRI_ERR_UNSUPPORTED) return rc;
+        // a batch beyond the engine's 32-bit descriptors: its own launch sequence below
+    }
     ktri_opts o{};
     o.struct_size = sizeof(ktri_opts);
     o.intersection_method = KTRI_METHOD_AUTO;
@@ -502,16 +610,7 @@ int launch_batch(ktri_server* s, Slot& sl) {
                                  reinterpret_cast<const uint64_t*>(dvf), k, reinterpret_cast<uint64_t*>(d + sl.off_tot),
                                  reinterpret_cast<uint64_t*>(d + sl.off_pv), &o, st);
     if (rc) return rc;
-    cudaMemcpyAsync(h + sl.h_tot, d + sl.off_tot, 8 * k, cudaMemcpyDeviceToHost, st);
-    if (sl.direct) {
-        const u64 warps = (n + 255) / 256;
-        const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
-        k_scatter_pv<<<blocks, 256, 0, st>>>(dsrc, dvf, k, n, reinterpret_cast<const u64*>(d + sl.off_pv));
-    } else {
-        cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
-    }
-    cudaEventRecord(sl.done, st);
-    return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
+    return enqueue_readback(s, sl);
 }
 
 // Harvest a finished slot (called with the lock held).
@@ -574,10 +673,41 @@ void worker_main(ktri_server* s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lock(s->mu);
     while (true) {
+        // batches the engine has counted: read them back
+        bool any_counting = false;
+        for (Slot& sl : s->slots) {
+            if (!(sl.busy && sl.counting)) continue;
+            const size_t j = slot_index(s, sl);
+            if (*(volatile unsigned long long*)(s->done_host + j) == sl.seq) {
+                sl.counting = false;
+                if (finish_engine_batch(s, sl) != KTRI_OK) {
+                    for (Request* r : sl.reqs) finish(s, r, KTRI_ERR_CUDA);
+                    sl.reqs.clear();
+                    sl.busy = false;
+                    s->cv_done.notify_all();
+                }
+            } else {
+                any_counting = true;
+            }
+        }
+        // a published job needs a running engine (one that was leaving as it was published
+        // is followed by a new launch)
+        if (any_counting && ensure_engine(s) != KTRI_OK) {
+            // the engine could not run: its batches fail (a device error is sticky, so the
+            // buffers are not reused by anything that could still run)
+            for (Slot& sl : s->slots) {
+                if (!(sl.busy && sl.counting)) continue;
+                for (Request* r : sl.reqs) finish(s, r, KTRI_ERR_CUDA);
+                sl.reqs.clear();
+                sl.counting = false;
+                sl.busy = false;
+            }
+            s->cv_done.notify_all();
+        }
         // finished batches
         bool any_busy = false;
         for (Slot& sl : s->slots) {
-            if (sl.busy && cudaEventQuery(sl.done) == cudaSuccess) {
+            if (sl.busy && !sl.counting && cudaEventQuery(sl.done) == cudaSuccess) {
                 harvest(s, sl);
                 s->cv_done.notify_all();
             }
@@ -689,7 +819,9 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
         if (opts->max_batch_nnz) s->opts.max_batch_nnz = opts->max_batch_nnz;
         if (opts->max_batch_graphs) s->opts.max_batch_graphs = opts->max_batch_graphs;
         s->opts.direct_host_access = opts->direct_host_access;
+        s->opts.engine = opts->engine;
     }
+    s->engine = s->opts.engine == 1;
     if (s->opts.slots > 8) s->opts.slots = 8;
     int pageable = 0;
     if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
@@ -711,6 +843,26 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
         cudaEventCreateWithFlags(&sl.cache_done, cudaEventDisableTiming);
     }
     cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+    if (rc == KTRI_OK && s->engine) {
+        // job records (zero: nothing published), the host-mapped completion words and the stop flag
+        void* hp = nullptr;
+        if (cudaMalloc(&s->jobs, sizeof(ktri::EngineJob) * s->slots.size()) != cudaSuccess ||
+            cudaMalloc(&s->stop_dev, sizeof(unsigned)) != cudaSuccess ||
+            cudaHostAlloc(&hp, sizeof(unsigned long long) * s->slots.size(), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->done_dev), hp, 0) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s->engine_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->engine_done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            rc = KTRI_ERR_CUDA;
+        } else {
+            s->done_host = static_cast<unsigned long long*>(hp);
+            std::memset(s->done_host, 0, sizeof(unsigned long long) * s->slots.size());
+            cudaMemset(s->jobs, 0, sizeof(ktri::EngineJob) * s->slots.size());
+            cudaMemset(s->stop_dev, 0, sizeof(unsigned));
+            s->engine_grid = ktri::engine_grid(ktri::ctx_num_sms(s->slots[0].ctx));
+            if (cudaDeviceSynchronize() != cudaSuccess) rc = KTRI_ERR_CUDA;
+        }
+    }
     if (rc == KTRI_OK) {
         // Reserve every slot's union buffer and pinned staging for a full batch (max_batch_nnz
         // entries over max_batch_nnz / 8 vertices) when all slots together take at most a
@@ -731,6 +883,7 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
     if (rc) {
         for (Slot& sl : s->slots)
             if (sl.ctx) ktri_ctx_destroy(sl.ctx);
+        release_engine(s);
         delete s;
         return rc;
     }
@@ -851,6 +1004,7 @@ int ktri_server_destroy(ktri_server* s) {
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(s->device);
+    release_engine(s);
     for (auto& kv : s->resident) cudaFreeAsync(kv.second.mem, s->aux);
     cudaStreamSynchronize(s->aux);
     for (Slot& sl : s->slots) {

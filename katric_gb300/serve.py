@@ -18,7 +18,8 @@ from .graph import Graph
 
 class Server:
     def __init__(self, device: int = 0, slots: int = 2, memory_budget: int = 120 << 30,
-                 max_batch_nnz: int = 1 << 28, max_batch_graphs: int = 4096, direct_host_access: bool = False):
+                 max_batch_nnz: int = 1 << 28, max_batch_graphs: int = 4096, direct_host_access: bool = False,
+                 engine: bool = False):
         self._L = _native.load()
         o = _native.ServerOpts()
         o.struct_size = ctypes.sizeof(_native.ServerOpts)
@@ -27,6 +28,7 @@ class Server:
         o.max_batch_nnz = max_batch_nnz
         o.max_batch_graphs = max_batch_graphs
         o.direct_host_access = 1 if direct_host_access else 0
+        o.engine = 1 if engine else 0
         h = ctypes.c_void_p()
         _native.check(self._L.ktri_server_create(device, ctypes.byref(o), ctypes.byref(h)))
         self._h = h

@@ -58,11 +58,13 @@ static int sizes(void) {
     FIELD(ktri_server_opts, max_batch_nnz);
     FIELD(ktri_server_opts, max_batch_graphs);
     FIELD(ktri_server_opts, direct_host_access);
+    FIELD(ktri_server_opts, engine);
     FIELD(ktri_server_opts, reserved);
     printf("ktri_server_stats %zu\n", sizeof(ktri_server_stats));
     FIELD(ktri_server_stats, submitted);
     FIELD(ktri_server_stats, coalesced);
     FIELD(ktri_server_stats, device_us);
+    FIELD(ktri_server_stats, engine_launches);
     FIELD(ktri_server_stats, reserved);
     printf("ktri_tuning %zu\n", sizeof(ktri_tuning));
     FIELD(ktri_tuning, intersection_method);

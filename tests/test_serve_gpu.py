@@ -1,6 +1,9 @@
 """Serving with continuous batching (needs a GB300): every result is the same alone and in
-the mix, repeats are answered from resident graphs, the memory budget is honoured."""
+the mix, repeats are answered from resident graphs, the memory budget is honoured, and with
+the engine batches published while the persistent counting kernel runs are counted by that
+same kernel."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -15,8 +18,8 @@ def graph_mix(count, seed):
     return [b.graph(i) for i in range(b.num_graphs)]
 
 
-@pytest.mark.parametrize("direct", [False, True])
-def test_results_alone_equal_results_in_the_mix(direct):
+@pytest.mark.parametrize("direct,engine", [(False, False), (True, False), (False, True), (True, True)])
+def test_results_alone_equal_results_in_the_mix(direct, engine):
     # besides the mix: a larger RMAT graph, an edgeless graph and a graph without vertices
     graphs = graph_mix(90, seed=31) + [Graph.rmat(15, 16, seed=3), Graph(np.zeros(5, np.uint64),
                                                                           np.zeros(0, np.uint32)),
@@ -24,7 +27,7 @@ def test_results_alone_equal_results_in_the_mix(direct):
     with TriangleCounter(0) as ctr:
         alone = [ctr.count(g.first_out, g.head) for g in graphs]
     # direct=True: on Grace + Blackwell the device gathers the graphs from host memory itself
-    with Server(slots=2, max_batch_nnz=1 << 18, direct_host_access=direct) as srv:
+    with Server(slots=2, max_batch_nnz=1 << 18, direct_host_access=direct, engine=engine) as srv:
         rids = [None] * len(graphs)
 
         def client(lo, hi):
@@ -106,3 +109,26 @@ def test_repeats_while_queued_join_the_count(direct):
         for rid, w in zip(later, [want_big] + want_small):
             total, pv, _ = srv.wait(rid)
             assert total == w[0] and np.array_equal(pv, w[1])
+
+
+def test_engine_folds_arrivals_into_the_running_kernel():
+    """Requests that arrive while the engine counts are prepared on a free slot and published
+    to the running engine: many batches, fewer engine launches, every result exact.  After the
+    stream dries up the engine leaves, and the next request launches it again."""
+    graphs = graph_mix(240, seed=13) + [Graph.rmat(16, 16, seed=s) for s in range(3)]
+    with TriangleCounter(0) as ctr:
+        alone = [ctr.count(g.first_out, g.head) for g in graphs]
+    with Server(slots=2, max_batch_nnz=1 << 17, engine=True) as srv:
+        rids = [srv.submit(g, key=0, borrow=True) for g in graphs]
+        for i, rid in enumerate(rids):
+            total, pv, _ = srv.wait(rid)
+            assert total == alone[i][0] and np.array_equal(pv, alone[i][1]), i
+        st = srv.stats()
+        assert st["batches"] >= 6
+        assert 1 <= st["engine_launches"] < st["batches"]
+        time.sleep(0.05)  # idle: the engine leaves
+        launches = st["engine_launches"]
+        rid = srv.submit(graphs[-1], key=0)
+        total, pv, _ = srv.wait(rid)
+        assert total == alone[-1][0] and np.array_equal(pv, alone[-1][1])
+        assert srv.stats()["engine_launches"] == launches + 1
