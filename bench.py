@@ -648,7 +648,7 @@ def main():
 
     for _ in range(3):
         e2e_step()
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 20))
     barrier()
     split = {"h2d": [], "d2h": [], "call": [], "orient": [], "count": [], "host_enqueue": [], "host_call": []}
     walls = []

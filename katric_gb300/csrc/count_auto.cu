@@ -502,10 +502,12 @@ __device__ __forceinline__ void chunk_sizes(u32 klen, u32 max_lg, u32 max_fl, u3
     *fl = f;
 }
 
-// One (owner, segment) tile of a large owner, counted by the whole block.  Returns true when a
-// bounded wait for a bulk copy ran out (inflight: the second wait ran out too).
+// One (owner, segment) tile of a large owner, counted by the whole block.  bar is the block's
+// bulk-copy mbarrier, initialised once and kept where no other use of shared memory reaches.
+// Returns true when a bounded wait for a bulk copy ran out (inflight: the second wait ran out too).
 template <int BLOCK, int CAP, typename OffT, bool CG = false>
-__device__ __forceinline__ bool large_tile(unsigned char* smem, uint2 tl, const u64* __restrict__ fo,
+__device__ __forceinline__ bool large_tile(unsigned char* smem, unsigned long long* bar, uint2 tl,
+                                           const u64* __restrict__ fo,
                                            const u32* __restrict__ head, u64 n, const Desc<OffT>* __restrict__ vdesc,
                                            const u32* __restrict__ headp, u32 seg, u64* __restrict__ cnt,
                                            u32 first_wait_polls, u32& phase, bool& inflight, u64& local_total,
@@ -528,7 +530,7 @@ __device__ __forceinline__ bool large_tile(unsigned char* smem, uint2 tl, const 
     u64* s_red = reinterpret_cast<u64*>(smem + L::off_red);
     u32& s_qn = *reinterpret_cast<u32*>(smem + L::off_qn);
     u32& s_next = *reinterpret_cast<u32*>(smem + L::off_next);
-    unsigned long long& s_bar = *reinterpret_cast<unsigned long long*>(smem + L::off_bar);
+    unsigned long long& s_bar = *bar;  // the block's bulk-copy barrier (its phase persists across tiles)
     bool timed_out = false;
     const u64 x = tl.x;
     const Desc<OffT> dxd = ld_desc<CG>(vdesc + x);
@@ -670,7 +672,7 @@ __global__ void __launch_bounds__(BLOCK) k_count_large(const u64* __restrict__ f
         __syncthreads();
         const u64 t = s_t;
         if (t >= ntiles) break;
-        timed_out = large_tile<BLOCK, CAP, OffT>(smem, ltiles[t], fo, head, n, vdesc, headp, seg, cnt,
+        timed_out = large_tile<BLOCK, CAP, OffT>(smem, s_bar, ltiles[t], fo, head, n, vdesc, headp, seg, cnt,
                                                  first_wait_polls, phase, inflight, local_total, dup);
         if (timed_out) break;
     }
@@ -964,8 +966,10 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
     __shared__ unsigned s_stop;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     (void)lane;
-    // the large-owner tiles' bulk-copy barrier lives in the large layout's scalar area
-    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(smem + EngineLargeL::off_bar);
+    // the large-owner tiles' bulk-copy barrier: outside the dynamic region, which the small- and
+    // medium-owner units overwrite between large tiles, since its phase persists across units
+    __shared__ __align__(8) unsigned long long s_bar_engine;
+    unsigned long long* s_bar = &s_bar_engine;
     if (threadIdx.x == 0) {
         mbar_init(s_bar, 1);
         s_jb.seq = 0;
@@ -1055,8 +1059,8 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
             }
         } else {
             const u64 t = u - jb->units_small - jb->units_medium;
-            timed_out = large_tile<BLOCK, LARGE_CAP, u32, true>(smem, __ldcg(jb->ltiles + t), jb->fo, jb->head, jb->n, vd,
-                                                                jb->headp,
+            timed_out = large_tile<BLOCK, LARGE_CAP, u32, true>(smem, s_bar, __ldcg(jb->ltiles + t), jb->fo, jb->head,
+                                                                jb->n, vd, jb->headp,
                                                           jb->seg, jb->cnt, COPY_WAIT_POLLS, phase, inflight,
                                                           unused_total, dup);
         }

@@ -132,3 +132,20 @@ def test_engine_folds_arrivals_into_the_running_kernel():
         total, pv, _ = srv.wait(rid)
         assert total == alone[-1][0] and np.array_equal(pv, alone[-1][1])
         assert srv.stats()["engine_launches"] == launches + 1
+
+
+def test_engine_mixes_large_owner_tiles_with_small_units():
+    """The engine's blocks take small-owner, medium and large-owner units of different jobs in
+    turn; a graph with large owners (out-degree above 256: bulk copies into shared memory) counted
+    among many small graphs must come out exact, per vertex."""
+    big = Graph.rmat(18, 16, seed=2)
+    graphs = graph_mix(120, seed=21)
+    mixed = graphs[:60] + [big] + graphs[60:] + [big]
+    with TriangleCounter(0) as ctr:
+        alone = [ctr.count(g.first_out, g.head) for g in mixed]
+    with Server(slots=2, max_batch_nnz=1 << 16, engine=True) as srv:
+        for rnd in range(2):
+            rids = [srv.submit(g, key=0, borrow=True) for g in mixed]
+            for i, rid in enumerate(rids):
+                total, pv, _ = srv.wait(rid)
+                assert total == alone[i][0] and np.array_equal(pv, alone[i][1]), (rnd, i)
