@@ -350,9 +350,11 @@ __global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ 
         atomicAdd(&hist[tile_key(fo, head, dplus, tiles[t], seg, shift, mode, keys, t)], 1u);
 }
 
-__global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
-    constexpr int PER = TILE_BUCKETS / 1024;
-    __shared__ u32 s_warp[32];
+// 256 threads: a block this small also fits beside the serving engine's resident blocks.
+constexpr int TILE_SCAN_BLOCK = 256;
+__global__ void __launch_bounds__(TILE_SCAN_BLOCK) k_tile_scan(u32* hist, Control* ctl) {
+    constexpr int PER = TILE_BUCKETS / TILE_SCAN_BLOCK;
+    __shared__ u32 s_warp[TILE_SCAN_BLOCK / 32];
     if (ctl->err & DEV_ERR_MASK) return;
     u32 v[PER], t = 0;
 #pragma unroll
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(1024) k_tile_scan(u32* hist, Control* ctl) {
         t += v[k];
     }
     u32 total;
-    u32 run = block_exclusive_scan<1024>(t, s_warp, &total);
+    u32 run = block_exclusive_scan<TILE_SCAN_BLOCK>(t, s_warp, &total);
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         hist[threadIdx.x * PER + k] = run;
@@ -397,7 +399,7 @@ void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n,
     if (mode == TILE_BY_COST)
         k_tile_cost<<<num_sms * 8, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, keys, ctl);
     k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, ctl);
-    k_tile_scan<<<1, 1024, 0, st>>>(hist, ctl);
+    k_tile_scan<<<1, TILE_SCAN_BLOCK, 0, st>>>(hist, ctl);
     k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, sorted,
                                                 ctl);
 }
