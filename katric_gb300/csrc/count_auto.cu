@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
                     // is done, which needs this unit
                     s_job = (int)j;
                     s_unit = cur & ENGINE_COUNT_MASK;
-                    start = j;
+                    start = j + 1;  // the next scan begins at the following job: no job is favoured
                     if (s_jb.seq == s1 && s_jb_slot == j) break;  // this block holds the record already
                     s_jb_slot = j;
                     s_jb.fo = vj->fo;
