@@ -12,8 +12,8 @@ namespace ktri {
 using u32 = uint32_t;
 using u64 = unsigned long long;
 
-constexpr int ORIENT_BLOCK = 128;
-constexpr int ORIENT_IPT = 6;
+constexpr int ORIENT_BLOCK = 256;   // 8 warps, one merge-path tile each
+constexpr int ORIENT_IPT = 8;       // slots per lane of a tile: tiles of 256 diagonals
 constexpr int SMALL_BLOCK = 256;
 constexpr int SMALL_D = 48;          // largest out-degree bound of the small-owner kernel's owners
 constexpr int SMALL_D_LOW = 32;      // bounds up to this run the small-owner kernel's instantiation for
@@ -29,13 +29,12 @@ constexpr u32 COPY_WAIT_POLLS = 1u << 22;  // polls of a bounded wait for a bulk
 constexpr u32 SMALL_WARP_DEG = 256;  // the small-owner kernel takes owners up to this degree; owners of
                                      // larger degree (and small out-degree) go to the medium kernel's tiles
 
-inline u64 spanning_capacity(u64 n, u64 nnz) { return (n + nnz) / (ORIENT_BLOCK * ORIENT_IPT) + 2; }
 // Merge-path tile boundaries are tabulated once per call at this granularity: entry k holds
-// the vertex where diagonal k * TILE_BASE crosses the path.  An orientation tile is one base
-// tile.
-constexpr u64 TILE_BASE = (u64)ORIENT_BLOCK * ORIENT_IPT;
-constexpr u64 ORIENT_PER_BASE = 1;
+// the vertex where diagonal k * TILE_BASE crosses the path.  One warp orients one base tile.
+constexpr u64 TILE_BASE = 32ull * ORIENT_IPT;
 inline u64 base_tiles(u64 n, u64 nnz) { return (n + nnz + TILE_BASE - 1) / TILE_BASE; }
+// Each base tile records at most one split list (the one that starts in it and ends past it).
+inline u64 spanning_capacity(u64 n, u64 nnz) { return base_tiles(n, nnz) + 2; }
 // Owners above small_d hold more than small_d adjacency entries each, and owners routed to the
 // tiles for their degree more than SMALL_WARP_DEG; every owner has at most deg / seg + 1 tiles.
 inline u64 large_tile_capacity(u64 n, u64 nnz, u32 small_d, u32 seg) {
@@ -76,10 +75,10 @@ struct TriangleSink {
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
                  int num_sms, cudaStream_t st);
-// Orientation over merge-path tiles [tile_begin, tile_end) of ORIENT_TILE items (all by
-// default).  Tile t reads adjacency slots below (t + 1) * ORIENT_TILE + 1 only, so it may run
-// as soon as that prefix of head is on the device.
-constexpr u64 ORIENT_TILE = TILE_BASE;
+// Orientation over the blocks [tile_begin, tile_end) of ORIENT_TILE diagonals (all by
+// default; a block holds ORIENT_BLOCK / 32 base tiles).  Block t reads adjacency slots below
+// (t + 1) * ORIENT_TILE + 1 only, so it may run as soon as that prefix of head is on the device.
+constexpr u64 ORIENT_TILE = (u64)ORIENT_BLOCK * ORIENT_IPT;
 u64 orient_tiles(u64 n, u64 nnz);
 void launch_orient(const u64* fo, const u32* head, u64 n, u64 nnz, const u32* deg, const u32* tile_i0, u32* headp,
                    u32* dplus, u32* spanning, Control* ctl, cudaStream_t st, u64 tile_begin = 0,

@@ -44,193 +44,156 @@ __global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restri
     if (err) atomicOr(&ctl->err, err);
 }
 
+// Orientation of one merge-path tile of W = 32 * IPT diagonals per warp.  The tile holds the
+// window vertices i0..i1 and the adjacency slots [j0, j1); every list with slots in the tile
+// has one piece there.  Slots are taken 32 at a time, one per lane, so the owner of a slot,
+// the rank of a kept entry among the tile's kept entries and a piece's count all come from
+// warp ballots and population counts: no block barrier, no per-thread path walk.
+//   vertex pass  at the slot where each piece starts: (window index + 1, degree of its vertex)
+//   pass 1       per slot: owner (the last piece start at or below the lane), deg[y] gather,
+//                the (deg, id) decision, input checks; at a piece's last slot its out-degree
+//                (a plain store, or an atomic reservation for a piece of a split list) and the
+//                gapped-array index of its first kept entry
+//   pass 2       kept entries written from registers, in slot order
+// A list held by one tile keeps its input order.  A split list's pieces reserve their ranges
+// with one atomic each and are recorded in the spanning list by the tile that holds the list's
+// start.
 template <int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, const u32* __restrict__ head, u64 n,
                                                   u64 nnz, const u32* __restrict__ deg,
                                                   const u32* __restrict__ tile_i0, u32* __restrict__ headp,
                                                   u32* __restrict__ dplus, u32* __restrict__ spanning,
                                                   Control* ctl, u64 tile_begin) {
-    constexpr int TILE = BLOCK * IPT;
-    // Everything inside a tile is addressed relative to its first vertex i0 and first slot j0,
-    // in 32 bits.  s_fo[k] = first_out[i0 + k] - j0 clamped to [0, nslot]: only the first
-    // vertex's start and the last one's end can lie outside the tile.
-    __shared__ u32 s_fo[TILE + 2];
-    __shared__ u32 s_deg[TILE + 2];
-    __shared__ u32 s_head[TILE];
-    __shared__ u32 s_cnt[TILE + 2];
-    __shared__ u32 s_first[TILE + 2];
-    __shared__ u32 s_warp[BLOCK / 32];
-    __shared__ u64 s_b[3];   // i0, i1, first_out[i0]
-    __shared__ u32 s_carry[2];
-    __shared__ u32 s_flags;  // bit 0: the last window vertex's list continues past the tile
+    constexpr int W = 32 * IPT;
+    constexpr int WARPS = BLOCK / 32;
+    constexpr u32 FULL = 0xFFFFFFFFu;
+    __shared__ uint2 s_info_all[WARPS][W];  // at a piece's first slot: (window index + 1, degree)
+    __shared__ u64 s_base_all[WARPS][W];    // at a piece's first slot: headp index of tile rank 0
 
     if (ctl->err & DEV_ERR_MASK) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const u64 total = n + nnz;
-    const u64 tile = tile_begin + blockIdx.x;
-    const u64 d0 = tile * TILE;
+    const u64 tile = (tile_begin + blockIdx.x) * WARPS + wid;
+    const u64 d0 = tile * W;
     if (d0 >= total) return;
-    const u64 d1 = d0 + TILE < total ? d0 + TILE : total;
-    if (threadIdx.x == 0) {
-        const u64 nt = (total + TILE_BASE - 1) / TILE_BASE;
-        const u64 k1 = ORIENT_PER_BASE * (tile + 1);
-        s_b[0] = tile_i0[ORIENT_PER_BASE * tile];
-        s_b[1] = tile_i0[k1 < nt ? k1 : nt];
-    }
-    __syncthreads();
-    const u64 i0 = s_b[0], i1 = s_b[1];
+    const u64 d1 = d0 + W < total ? d0 + W : total;
+    uint2* s_info = s_info_all[wid];
+    u64* s_base = s_base_all[wid];
+    // tile_i0 holds base_tiles + 1 entries (the last is n), and tile + 1 <= base_tiles here
+    const u64 i0 = tile_i0[tile], i1 = tile_i0[tile + 1];
     const u64 j0 = d0 - i0, j1 = d1 - i1;
-    const u32 nslot = (u32)(j1 - j0);
-    const u32 last = (u32)(i1 - i0);  // window vertices 0..last (last may be n - i0: no vertex)
-    const u64 fo_last = i1 + 1 < n ? i1 + 1 : n;
-    const u32 nfo = (u32)(fo_last - i0 + 1);
-    for (u32 k = threadIdx.x; k < nfo; k += BLOCK) {
-        const u64 f = fo[i0 + k];
-        s_fo[k] = f < j0 ? 0u : (f > j1 ? nslot : (u32)(f - j0));
-        s_cnt[k] = 0;
-        if (k <= last && i0 + k < n) s_deg[k] = deg[i0 + k];
-        if (k == 0) s_b[2] = f;
+    const u32 ns = (u32)(j1 - j0);
+    if (ns == 0) return;  // only vertex ends: those lists have no slots here (out-degrees start at 0)
+    // every slot's neighbour and its degree, all in flight before the window is read
+    u32 y_r[IPT], dy_r[IPT];
+#pragma unroll
+    for (int it = 0; it < IPT; ++it) {
+        const u32 s = (u32)it * 32 + lane;
+        y_r[it] = s < ns ? __ldcs(head + j0 + s) : 0u;
     }
-    if (nfo <= last + 1) s_fo[last + 1] = nslot;  // the window ends at n
-    for (u32 k = threadIdx.x; k < nslot; k += BLOCK) s_head[k] = head[j0 + k];
-    if (threadIdx.x == 0) s_flags = (i1 < n && fo[i1 + 1] > j1) ? 1u : 0u;
-    __syncthreads();
-
-    // this thread's run of the merge path: items t .. te of the tile
-    const u32 t = threadIdx.x * IPT < (u32)(d1 - d0) ? threadIdx.x * IPT : (u32)(d1 - d0);
-    const u32 te = t + IPT < (u32)(d1 - d0) ? t + IPT : (u32)(d1 - d0);
-    u32 i_start;  // largest i in [0, last] with s_fo[i] + i <= t
+#pragma unroll
+    for (int it = 0; it < IPT; ++it) {
+        const u32 s = (u32)it * 32 + lane;
+        dy_r[it] = (s < ns && (u64)y_r[it] < n) ? __ldg(deg + y_r[it]) : 0u;
+    }
+    for (u32 s = lane; s < ns; s += 32) s_info[s] = make_uint2(0u, 0u);
+    __syncwarp();
+    const u64 last_v = i1 < n ? i1 : n - 1;
+    const u32 nwin = (u32)(last_v - i0) + 1;  // window vertices (at most W + 1)
+    u64 fo_i0;
     {
-        u32 lo = 0, hi = last;
-        while (lo < hi) {
-            const u32 mid = (lo + hi + 1) >> 1;
-            if (s_fo[mid] + mid <= t) lo = mid;
-            else hi = mid - 1;
-        }
-        i_start = lo;
+        // the first 32 window vertices with every lane present, so lane 0's start is shared
+        const bool have = (u32)lane < nwin;
+        const u64 a = have ? fo[i0 + lane] : 0, b = have ? fo[i0 + lane + 1] : 0;
+        fo_i0 = __shfl_sync(FULL, a, 0);
+        if (have && b > a && a < j1 && b > j0)
+            s_info[a > j0 ? a - j0 : 0] = make_uint2((u32)lane + 1, (u32)(b - a));
     }
-    const u32 j_start = t - i_start;
-    const u32 nv = (u32)(n - i0);  // window vertices that exist: i < nv
+    for (u32 k = 32 + lane; k < nwin; k += 32) {
+        const u64 v = i0 + k;
+        const u64 a = fo[v], b = fo[v + 1];
+        if (b > a && a < j1 && b > j0) s_info[a - j0] = make_uint2(k + 1, (u32)(b - a));
+    }
+    __syncwarp();
+    const bool first_before = fo_i0 < j0;  // the first piece continues a list begun before the tile
+    const u32 lt = (1u << lane) - 1u, le = lt | (1u << lane);
 
-    u32 own[IPT], yv[IPT];
-    bool unsorted = false;
+    u32 s0_r[IPT], km_r[IPT];
+    u32 rank = 0;                          // kept entries of the tile before this iteration
+    u32 s0c = 0, kc = 0, dc = 0, pc = 0;   // the piece open at the end of the previous iteration
     u32 err = 0;
-    {
-        u32 i = i_start, j = j_start;
+    bool unsorted = false;
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            own[k] = NONE;
-            yv[k] = 0;
-            if (t + k < te) {
-                if (i < nv && j < s_fo[i + 1]) {
-                    own[k] = i;
-                    const u32 y = s_head[j];
-                    yv[k] = y;
-                    u32 nx = y;
-                    bool has_next = false;
-                    if (j + 1 < s_fo[i + 1]) {
-                        nx = s_head[j + 1];
-                        has_next = true;
-                    } else if (i == last && (s_flags & 1u) && j + 1 == nslot) {
-                        nx = __ldg(head + j0 + nslot);
-                        has_next = true;
-                    }
-                    if (has_next) {
-                        if (nx < y) unsorted = true;
-                        if (nx == y) err |= DEV_ERR_DUPLICATE;
-                    }
-                    ++j;
-                } else {
-                    ++i;
-                }
-            }
-        }
-    }
-    u32 dy[IPT];
-#pragma unroll
-    for (int k = 0; k < IPT; ++k) dy[k] = (own[k] != NONE && yv[k] < n) ? __ldg(deg + yv[k]) : 0u;
-
-    u32 outbits = 0;
-    {
-        u32 run_owner = NONE, run = 0;
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            if (own[k] == NONE) continue;
-            const u64 x = i0 + own[k];
-            const u32 y = yv[k];
-            bool out = false;
-            if (y >= n) err |= DEV_ERR_ID_RANGE;
+    for (int it = 0; it < IPT; ++it) {
+        s0_r[it] = 0;
+        km_r[it] = 0;
+        if ((u32)it * 32 >= ns) continue;
+        const u32 s = (u32)it * 32 + lane;
+        const bool valid = s < ns;
+        const uint2 info = valid ? s_info[s] : make_uint2(0u, 0u);
+        const u32 starts = __ballot_sync(FULL, info.x != 0);
+        const u32 below = starts & le;
+        const int src = 31 - __clz(below);  // -1 when no piece starts at or below this lane
+        const u32 kx = __shfl_sync(FULL, info.x, src & 31);
+        const u32 dxs = __shfl_sync(FULL, info.y, src & 31);
+        const bool here = below != 0;
+        const u32 s0 = here ? (u32)it * 32 + (u32)src : s0c;
+        const u32 k1 = here ? kx : kc;
+        const u32 dx = here ? dxs : dc;
+        const u32 y = y_r[it];
+        const u64 x = i0 + k1 - 1;
+        bool kept = false;
+        if (valid) {
+            if ((u64)y >= n) err |= DEV_ERR_ID_RANGE;
             else if ((u64)y == x) err |= DEV_ERR_SELF_LOOP;
-            else out = key_less(s_deg[own[k]], x, dy[k], y);
-            if (own[k] != run_owner) {
-                if (run) atomicAdd(&s_cnt[run_owner], run);
-                run_owner = own[k];
-                run = 0;
-            }
-            if (out) {
-                outbits |= 1u << k;
-                ++run;
-            }
+            else kept = key_less(dx, x, dy_r[it], y);
         }
-        if (run) atomicAdd(&s_cnt[run_owner], run);
+        const u32 km = __ballot_sync(FULL, kept);
+        const u32 pst = here ? rank + __popc(km & ((1u << (src & 31)) - 1u)) : pc;  // rank at the piece start
+        const u64 a = (k1 == 1 && first_before) ? fo_i0 : j0 + s0;
+        const u64 b = a + dx;
+        const bool last_slot = s + 1 == ns;
+        bool next_start;
+        if (lane < 31) next_start = (starts >> (lane + 1)) & 1u;
+        else next_start = valid && !last_slot && s_info[s + 1].x != 0;
+        // the next slot's neighbour: the next lane's, or lane 0's of the next iteration
+        const u32 nd = __shfl_down_sync(FULL, y, 1);
+        const u32 nn = __shfl_sync(FULL, y_r[it + 1 < IPT ? it + 1 : it], 0);
+        if (valid && (last_slot ? b > j1 : !next_start)) {
+            // the next slot holds the same list: adjacent duplicates and order
+            const u32 nx = last_slot ? __ldcs(head + j1) : (lane < 31 ? nd : nn);
+            if (nx < y) unsorted = true;
+            if (nx == y) err |= DEV_ERR_DUPLICATE;
+        }
+        if (valid && (last_slot || next_start)) {
+            // the piece's last slot in the tile: its out-degree share and its entries' place
+            const u32 cnt = rank + __popc(km & le) - pst;
+            u32 carry = 0;
+            if (a < j0 || b > j1) {
+                if (cnt) carry = atomicAdd(&dplus[x], cnt);
+                if (a >= j0) spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)x;
+            } else {
+                dplus[x] = cnt;
+            }
+            s_base[s0] = oriented_start(a, x) + carry - pst;
+        }
+        s0c = __shfl_sync(FULL, s0, 31);
+        kc = __shfl_sync(FULL, k1, 31);
+        dc = __shfl_sync(FULL, dx, 31);
+        pc = __shfl_sync(FULL, pst, 31);
+        rank += __popc(km);
+        s0_r[it] = s0;
+        km_r[it] = km;
     }
     if (err) atomicOr(&ctl->err, err);
     if (unsorted) atomicOr(&ctl->err, DEV_FLAG_UNSORTED);
-
-    u32 tot;
-    const u32 base = block_exclusive_scan<BLOCK>((u32)__popc(outbits), s_warp, &tot);
-
-    // first in-tile slot of every owner: record its scan position; lists wholly inside the
-    // tile (every window vertex but possibly the first and the last) publish their out-degree
-    const bool first_whole = s_b[2] >= j0 && (last > 0 || !(s_flags & 1u));
-    {
-        u32 run = base;
-        u32 j = j_start;
+    __syncwarp();
+    rank = 0;
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            if (own[k] == NONE) continue;
-            const u32 o = own[k];
-            if (j == s_fo[o]) {
-                s_first[o] = run;
-                const bool whole = o == 0 ? first_whole : (o < last || !(s_flags & 1u));
-                if (whole) dplus[i0 + o] = s_cnt[o];
-            }
-            if (outbits >> k & 1u) ++run;
-            ++j;
-        }
-    }
-    if (threadIdx.x == 0) {
-        s_carry[0] = 0;
-        s_carry[1] = 0;
-        if (i0 < n) {
-            const u64 a = fo[i0], b = fo[i0 + 1];
-            const u64 lo = a > j0 ? a : j0, hi = b < j1 ? b : j1;
-            if (lo < hi && (a < j0 || b > j1)) {
-                s_carry[0] = atomicAdd(&dplus[i0], s_cnt[0]);
-                if (a >= j0) spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)i0;
-            }
-        }
-        if (i1 != i0 && i1 < n) {
-            const u64 a = fo[i1], b = fo[i1 + 1];
-            if (a < j1 && b > j1) {
-                s_carry[1] = atomicAdd(&dplus[i1], s_cnt[last]);
-                spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)i1;
-            }
-        }
-    }
-    __syncthreads();
-    {
-        u32 run = base;
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            if (!(outbits >> k & 1u)) continue;
-            const u32 o = own[k];
-            const u32 carry = o == 0 ? s_carry[0] : (o == last ? s_carry[1] : 0u);
-            const u32 pos = run - s_first[o] + carry;
-            // every window vertex after the first starts inside the tile, at j0 + s_fo[o]
-            const u64 fx = o == 0 ? s_b[2] : j0 + s_fo[o];
-            headp[oriented_start(fx, i0 + o) + pos] = yv[k];
-            ++run;
-        }
+    for (int it = 0; it < IPT; ++it) {
+        const u32 km = km_r[it];
+        if ((km >> lane) & 1u) __stcs(headp + s_base[s0_r[it]] + rank + __popc(km & lt), y_r[it]);
+        rank += __popc(km);
     }
 }
 
