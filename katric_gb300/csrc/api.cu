@@ -30,6 +30,7 @@ struct ktri_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;  // stream of the host-buffer entry points
+    int pageable_access = 0;        // kernels may address pageable host memory
     void* ws = nullptr;             // grow-only device workspace
     size_t ws_bytes = 0;
     uint64_t budget = 0;
@@ -225,6 +226,35 @@ struct EnginePublish {
     unsigned long long seq = 0;
     unsigned long long* done_word = nullptr;  // device address of the host-mapped completion word
 };
+
+// The address under which the device reads or writes a caller's host buffer, or nullptr when
+// only the copy engines reach it: pinned and registered memory through its device pointer,
+// pageable memory directly where the platform lets kernels address it.
+const void* device_view(const ktri_ctx* ctx, const void* host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered && ctx->pageable_access) return host;
+    return nullptr;
+}
+
+// Host -> device (to_device) or device -> host copy of a caller's buffer on stream st: by a
+// kernel where the device can address the host side and both ends are 16-byte aligned (or the
+// copy is at most 256 bytes), otherwise by the copy engines.  The kernel copies avoid the copy
+// engines' recurring slow windows on this platform.
+cudaError_t copy_host(ktri_ctx* ctx, void* dst, const void* src, size_t bytes, bool to_device, cudaStream_t st) {
+    if (bytes == 0) return cudaSuccess;
+    const void* view = device_view(ctx, to_device ? src : dst);
+    if (view) {
+        const void* from = to_device ? view : src;
+        void* to = to_device ? dst : const_cast<void*>(view);
+        if (ktri::launch_copy(from, to, bytes, ctx->num_sms, st)) return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, st);
+}
 
 // Polls of the large-owner kernel's first bulk-copy wait for an option value.
 u32 first_wait_polls(uint32_t opt) {
@@ -577,6 +607,10 @@ int ktri_ctx_create(int device, ktri_ctx** out) {
     ctx->device = device;
     DeviceGuard g(device);
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        ctx->pageable_access = 0;
+        cudaGetLastError();
+    }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return KTRI_ERR_CUDA;
@@ -725,7 +759,7 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
     auto* d_total = reinterpret_cast<u64*>(base + L.total);
     cudaStream_t st = ctx->stream;
     KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[0], st));
-    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, copy_host(ctx, d_fo, first_out, sizeof(u64) * (n + 1), true, st));
     // head in pieces on the copy stream; the orientation tiles of each piece start on the
     // counting stream as soon as it has landed, so the copy hides the orientation
     HeadChunks chunks;
@@ -742,8 +776,7 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
         KTRI_CK(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_free, 0));
         u64 b = 0;
         for (size_t c = 0; c < ends.size(); ++c) {
-            KTRI_CK(ctx, cudaMemcpyAsync(d_head + b, head + b, sizeof(u32) * (ends[c] - b), cudaMemcpyHostToDevice,
-                                         ctx->copy_stream));
+            KTRI_CK(ctx, copy_host(ctx, d_head + b, head + b, sizeof(u32) * (ends[c] - b), true, ctx->copy_stream));
             KTRI_CK(ctx, cudaEventRecord(ctx->chunk_ev[c], ctx->copy_stream));
             b = ends[c];
         }
@@ -752,7 +785,7 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
         chunks.ends = ends.data();
         chunks.events = ctx->chunk_ev.data();
     } else {
-        if (nnz) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, head_bytes, cudaMemcpyHostToDevice, st));
+        if (nnz) KTRI_CK(ctx, copy_host(ctx, d_head, head, head_bytes, true, st));
         KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[1], st));
     }
     rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false, {},
@@ -761,9 +794,8 @@ int ktri_count_csr_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
                                     chunks.count ? &chunks : nullptr);
     if (rc) return rc;
     KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[2], st));
-    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
-    if (per_vertex_out)
-        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, copy_host(ctx, total_out, d_total, sizeof(u64), false, st));
+    if (per_vertex_out) KTRI_CK(ctx, copy_host(ctx, per_vertex_out, d_cnt, sizeof(u64) * n, false, st));
     KTRI_CK(ctx, cudaEventRecord(ctx->ev_io[3], st));
     ctx->have_io = true;
     const auto t_enqueued = std::chrono::steady_clock::now();
@@ -883,10 +915,10 @@ int ktri_count_binary_file(ktri_ctx* ctx, const char* stem, uint64_t* total_out,
                 if (off == 0) fo_first = *static_cast<const u64*>(pinned[slot]);
                 if (off + len == bytes)
                     fo_last = *reinterpret_cast<const u64*>(static_cast<const char*>(pinned[slot]) + len - 8);
-                KTRI_CK(ctx, cudaMemcpyAsync(dst + off, pinned[slot], len, cudaMemcpyHostToDevice, st));
+                KTRI_CK(ctx, copy_host(ctx, dst + off, pinned[slot], len, true, st));
             } else {
                 char* sdev = stage + (size_t)slot * chunk_bytes;
-                KTRI_CK(ctx, cudaMemcpyAsync(sdev, pinned[slot], len, cudaMemcpyHostToDevice, st));
+                KTRI_CK(ctx, copy_host(ctx, sdev, pinned[slot], len, true, st));
                 ktri::launch_narrow_ids(reinterpret_cast<const u64*>(sdev), len / 8,
                                         reinterpret_cast<u32*>(dst) + off / 8, ctx->num_sms, st);
             }
@@ -905,9 +937,8 @@ int ktri_count_binary_file(ktri_ctx* ctx, const char* stem, uint64_t* total_out,
     rc = L.wide ? run_pipeline<u64>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false)
                 : run_pipeline<u32>(ctx, L, d_fo, d_head, n, nnz, d_total, d_cnt, opt, st, false);
     if (rc) return cleanup(rc);
-    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
-    if (per_vertex_out)
-        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, copy_host(ctx, total_out, d_total, sizeof(u64), false, st));
+    if (per_vertex_out) KTRI_CK(ctx, copy_host(ctx, per_vertex_out, d_cnt, sizeof(u64) * n, false, st));
     rc = device_status(ctx);
     if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
     return cleanup(rc);
@@ -1174,16 +1205,15 @@ int ktri_count_dag_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_t*
     auto* d_cnt = reinterpret_cast<u64*>(base + L.cnt);
     auto* d_total = reinterpret_cast<u64*>(base + L.total);
     cudaStream_t st = ctx->stream;
-    KTRI_CK(ctx, cudaMemcpyAsync(dfo, first_out, sizeof(u64) * (n + 1), cudaMemcpyHostToDevice, st));
-    if (m) KTRI_CK(ctx, cudaMemcpyAsync(dhead, head, sizeof(u32) * m, cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, copy_host(ctx, dfo, first_out, sizeof(u64) * (n + 1), true, st));
+    if (m) KTRI_CK(ctx, copy_host(ctx, dhead, head, sizeof(u32) * m, true, st));
     ktri::launch_dag_symmetrize(dfo, dhead, n, fs, hs, cursor, sums, ctx->num_sms, st);
     KTRI_CK(ctx, cudaGetLastError());
     rc = L.wide ? run_pipeline<u64>(ctx, L, fs, hs, n, nnz, d_total, d_cnt, opt, st, false)
                 : run_pipeline<u32>(ctx, L, fs, hs, n, nnz, d_total, d_cnt, opt, st, false);
     if (rc) return rc;
-    KTRI_CK(ctx, cudaMemcpyAsync(total_out, d_total, sizeof(u64), cudaMemcpyDeviceToHost, st));
-    if (per_vertex_out)
-        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n, cudaMemcpyDeviceToHost, st));
+    KTRI_CK(ctx, copy_host(ctx, total_out, d_total, sizeof(u64), false, st));
+    if (per_vertex_out) KTRI_CK(ctx, copy_host(ctx, per_vertex_out, d_cnt, sizeof(u64) * n, false, st));
     rc = device_status(ctx);
     if (rc == KTRI_OK) ctx->stats.triangles = *total_out;
     return rc;
@@ -1300,18 +1330,17 @@ int ktri_count_batch_ctx(ktri_ctx* ctx, const uint64_t* first_out, const uint32_
     auto* d_gf = reinterpret_cast<u64*>(base + off_gf);
     auto* d_tot = reinterpret_cast<u64*>(base + off_tot);
     cudaStream_t st = ctx->stream;
-    KTRI_CK(ctx, cudaMemcpyAsync(d_fo, first_out, sizeof(u64) * (n_total + 1), cudaMemcpyHostToDevice, st));
-    if (nnz_total) KTRI_CK(ctx, cudaMemcpyAsync(d_head, head, sizeof(u32) * nnz_total, cudaMemcpyHostToDevice, st));
-    KTRI_CK(ctx, cudaMemcpyAsync(d_gf, graph_first, sizeof(u64) * (num_graphs + 1), cudaMemcpyHostToDevice, st));
+    KTRI_CK(ctx, copy_host(ctx, d_fo, first_out, sizeof(u64) * (n_total + 1), true, st));
+    if (nnz_total) KTRI_CK(ctx, copy_host(ctx, d_head, head, sizeof(u32) * nnz_total, true, st));
+    KTRI_CK(ctx, copy_host(ctx, d_gf, graph_first, sizeof(u64) * (num_graphs + 1), true, st));
     rc = L.wide ? enqueue_batch<u64>(ctx, base, L, d_fo, d_head, n_total, nnz_total, d_gf, num_graphs, d_tot, d_cnt,
                                      opt, st, true)
                 : enqueue_batch<u32>(ctx, base, L, d_fo, d_head, n_total, nnz_total, d_gf, num_graphs, d_tot, d_cnt,
                                      opt, st, true);
     if (rc) return rc;
     note_pending(ctx, L, base, st, n_total, nnz_total, opt);
-    if (num_graphs) KTRI_CK(ctx, cudaMemcpyAsync(totals_out, d_tot, sizeof(u64) * num_graphs, cudaMemcpyDeviceToHost, st));
-    if (per_vertex_out)
-        KTRI_CK(ctx, cudaMemcpyAsync(per_vertex_out, d_cnt, sizeof(u64) * n_total, cudaMemcpyDeviceToHost, st));
+    if (num_graphs) KTRI_CK(ctx, copy_host(ctx, totals_out, d_tot, sizeof(u64) * num_graphs, false, st));
+    if (per_vertex_out) KTRI_CK(ctx, copy_host(ctx, per_vertex_out, d_cnt, sizeof(u64) * n_total, false, st));
     return device_status(ctx);
 }
 

@@ -116,6 +116,16 @@ __device__ __forceinline__ u32 bucket_probe16(const u32* keys, u32* hits32, u32 
     return 0u;
 }
 
+// Index of the segment holding item base + lane, for segments that start at strictly increasing
+// positions: before = segments started at or below base (at least one), starts = bit p set when
+// a segment starts at base + p (p in 1..31).
+__device__ __forceinline__ u32 segment_of(u32 before, u32 starts, u32 le_mask) {
+    return before - 1 + __popc(starts & le_mask);
+}
+// Bit (s - base) for a segment start s inside (base, base + 32), else 0.
+__device__ __forceinline__ u32 start_bit(bool have, u32 s, u32 base) {
+    return (have && s > base && s < base + 32) ? 1u << (s - base) : 0u;
+}
 
 // The same lookup without early exits: one bucket read, a walk along full buckets only when
 // the home bucket is full and holds no w (rare at the tables' load factors), and a predicated
@@ -253,13 +263,17 @@ __device__ __forceinline__ void small_batch(u32* base, u64 bi, const u64* __rest
         for (u32 i = lane; i < T / 2; i += 32) hitc[i] = 0;
         for (u32 i = lane; i < 64; i += 32) bins[i] = 0;
         __syncwarp();
+        // member lane (< G) holds its key and adjacency prefixes: owners of items by start masks
+        const u32 le_mask = lt_mask | (1u << lane);
+        const bool mem = (u32)lane < G;
+        const u32 kst = mem ? own[OW * lane + 3] : 0u, ast = mem ? own[OW * lane + 4] : 0u;
         // keys of every owner of the group
-        for (u32 q = lane; q < K; q += 32) {
-            u32 gi = 0;
-#pragma unroll
-            for (int g = 1; g < L::GROUP; ++g)
-                if ((u32)g < G && own[OW * g + 3] <= q) gi = g;
-            const u32* o = own + OW * gi;
+        for (u32 q0 = 0; q0 < K; q0 += 32) {
+            const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, mem && kst <= q0));
+            const u32 starts = __reduce_or_sync(0xFFFFFFFFu, start_bit(mem, kst, q0));
+            const u32 q = q0 + lane;
+            if (q >= K) continue;
+            const u32* o = own + OW * segment_of(before, starts, le_mask);
             const u64 xs = (u64)o[8] | ((u64)o[9] << 32);
             if (!bucket_insert(keys + (o[1] >> 5), o[1] & 31u, ld_in<CG>(headp + xs + (q - o[3])))) dup = 1;
         }
@@ -269,14 +283,14 @@ __device__ __forceinline__ void small_batch(u32* base, u64 bi, const u64* __rest
             u32 yv[4], gv[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const u32 e = e0 + 32 * u + lane;
+                const u32 eb = e0 + 32 * u;
+                const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, mem && ast <= eb));
+                const u32 starts = __reduce_or_sync(0xFFFFFFFFu, start_bit(mem, ast, eb));
+                const u32 e = eb + lane;
                 yv[u] = NONE;
                 gv[u] = 0;
                 if (e < D) {
-                    u32 gi = 0;
-#pragma unroll
-                    for (int g = 1; g < L::GROUP; ++g)
-                        if ((u32)g < G && own[OW * g + 4] <= e) gi = g;
+                    const u32 gi = segment_of(before, starts, le_mask);
                     const u64 xa = (u64)own[OW * gi + 6] | ((u64)own[OW * gi + 7] << 32);
                     gv[u] = gi;
                     yv[u] = ld_in<CG>(head + xa + (e - own[OW * gi + 4]));

@@ -95,8 +95,9 @@ void launch_desc(const u64* fo, u64 n, const u32* dplus, void* vdesc, uint2* mti
 // TILE_BY_VERTEX, the first vertex each segment streams (tiles that run together then stream
 // from the same region of the list array); TILE_BY_DEGREE, the owner's out-degree, largest
 // first; TILE_BY_COST, the tile's streamed entries (k_tile_cost writes them, log-scaled, into
-// keys, which needs the tiles' capacity in u32), heaviest first.  hist needs
-// tile_order_scratch_words() u32, sorted the same capacity as tiles.
+// keys), heaviest first.  keys holds every tile's key between the two passes, so it needs the
+// tiles' capacity in u32; hist needs tile_order_scratch_words() u32, sorted the same capacity
+// as tiles.
 enum : u32 { TILE_BY_VERTEX = 0, TILE_BY_DEGREE = 1, TILE_BY_COST = 2 };
 u64 tile_order_scratch_words();
 void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n, const uint2* tiles,
@@ -167,6 +168,11 @@ void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, c
 
 // u64 ids (the binary file format) -> u32 ids; ids above 2^32 - 1 become 0xFFFFFFFF.
 void launch_narrow_ids(const u64* src, u64 count, u32* dst, int num_sms, cudaStream_t st);
+// bytes from src to dst by a kernel (either side may be host memory the device can address).
+// Both addresses 16-byte aligned (copy_by_kernel_ok), or at most 256 bytes; false (nothing
+// launched) otherwise.
+bool copy_by_kernel_ok(const void* src, const void* dst);
+bool launch_copy(const void* src, void* dst, u64 bytes, int num_sms, cudaStream_t st);
 
 // Oriented out-lists -> undirected CSR of their edges (fs: n + 1 offsets, hs: 2m ids).  cursor
 // needs n u32 and sums dag_scan_chunks(n) u64 of scratch.

@@ -303,14 +303,42 @@ __global__ void k_tile_cost(const u64* __restrict__ fo, const u32* __restrict__ 
     }
 }
 
-__global__ void k_tile_hist(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
-                            const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
-                            u32 mode, const u32* __restrict__ keys, u32* hist, Control* ctl) {
+// Tiles [t0, t1) of block b when the tiles are cut into gridDim.x contiguous chunks.
+__device__ __forceinline__ void tile_chunk(u64 nt, u64& t0, u64& t1) {
+    const u64 per = (nt + gridDim.x - 1) / gridDim.x;
+    t0 = (u64)blockIdx.x * per;
+    t1 = t0 + per < nt ? t0 + per : nt;
+    if (t0 > t1) t0 = t1;
+}
+
+// Histogram of the tiles' keys.  Each block counts its contiguous chunk in shared memory and
+// adds the non-zero counts to the global histogram (one atomic per key present in the chunk,
+// not per tile: the medium tiles' degree keys crowd onto a few hundred values).  The keys are
+// left in keys[t] for the scatter (TILE_BY_COST finds them there already).
+constexpr int TILE_ORDER_BLOCK = 256;
+__global__ void __launch_bounds__(TILE_ORDER_BLOCK) k_tile_hist(const u64* __restrict__ fo,
+                                                                const u32* __restrict__ head,
+                                                                const u32* __restrict__ dplus,
+                                                                const uint2* __restrict__ tiles,
+                                                                const unsigned long long* count, u32 seg, u32 shift,
+                                                                u32 mode, u32* __restrict__ keys, u32* hist,
+                                                                Control* ctl) {
+    __shared__ u32 s_cnt[TILE_BUCKETS];
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
-    const u64 stride = (u64)gridDim.x * blockDim.x;
-    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride)
-        atomicAdd(&hist[tile_key(fo, head, dplus, tiles[t], seg, shift, mode, keys, t)], 1u);
+    u64 t0, t1;
+    tile_chunk(nt, t0, t1);
+    if (t0 == t1) return;
+    for (u32 k = threadIdx.x; k < TILE_BUCKETS; k += TILE_ORDER_BLOCK) s_cnt[k] = 0;
+    __syncthreads();
+    for (u64 t = t0 + threadIdx.x; t < t1; t += TILE_ORDER_BLOCK) {
+        const u32 key = tile_key(fo, head, dplus, tiles[t], seg, shift, mode, keys, t);
+        if (mode != TILE_BY_COST) keys[t] = key;
+        atomicAdd(&s_cnt[key], 1u);
+    }
+    __syncthreads();
+    for (u32 k = threadIdx.x; k < TILE_BUCKETS; k += TILE_ORDER_BLOCK)
+        if (s_cnt[k]) atomicAdd(&hist[k], s_cnt[k]);
 }
 
 // 256 threads: a block this small also fits beside the serving engine's resident blocks.
@@ -334,17 +362,29 @@ __global__ void __launch_bounds__(TILE_SCAN_BLOCK) k_tile_scan(u32* hist, Contro
     }
 }
 
-__global__ void k_tile_scatter(const u64* __restrict__ fo, const u32* __restrict__ head, const u32* __restrict__ dplus,
-                               const uint2* __restrict__ tiles, const unsigned long long* count, u32 seg, u32 shift,
-                               u32 mode, const u32* __restrict__ keys, u32* cursor, uint2* __restrict__ sorted,
-                               Control* ctl) {
+// Scatter of the tiles into key order (cursor = the scanned histogram).  Each block counts its
+// chunk's keys again, reserves one range per key present with one atomic, and hands out the
+// positions inside its ranges with shared-memory atomics.
+__global__ void __launch_bounds__(TILE_ORDER_BLOCK) k_tile_scatter(const uint2* __restrict__ tiles,
+                                                                   const unsigned long long* count,
+                                                                   const u32* __restrict__ keys, u32* cursor,
+                                                                   uint2* __restrict__ sorted, Control* ctl) {
+    __shared__ u32 s_pos[TILE_BUCKETS];
     if (ctl->err & DEV_ERR_MASK) return;
     const u64 nt = *(volatile const unsigned long long*)count;
-    const u64 stride = (u64)gridDim.x * blockDim.x;
-    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) {
-        const uint2 tl = tiles[t];
-        sorted[atomicAdd(&cursor[tile_key(fo, head, dplus, tl, seg, shift, mode, keys, t)], 1u)] = tl;
+    u64 t0, t1;
+    tile_chunk(nt, t0, t1);
+    if (t0 == t1) return;
+    for (u32 k = threadIdx.x; k < TILE_BUCKETS; k += TILE_ORDER_BLOCK) s_pos[k] = 0;
+    __syncthreads();
+    for (u64 t = t0 + threadIdx.x; t < t1; t += TILE_ORDER_BLOCK) atomicAdd(&s_pos[keys[t]], 1u);
+    __syncthreads();
+    for (u32 k = threadIdx.x; k < TILE_BUCKETS; k += TILE_ORDER_BLOCK) {
+        const u32 c = s_pos[k];
+        if (c) s_pos[k] = atomicAdd(&cursor[k], c);
     }
+    __syncthreads();
+    for (u64 t = t0 + threadIdx.x; t < t1; t += TILE_ORDER_BLOCK) sorted[atomicAdd(&s_pos[keys[t]], 1u)] = tiles[t];
 }
 
 // ---- launchers ------------------------------------------------------------------------
@@ -361,10 +401,10 @@ void launch_order_tiles(const u64* fo, const u32* head, const u32* dplus, u64 n,
     cudaMemsetAsync(hist, 0, sizeof(u32) * TILE_BUCKETS, st);
     if (mode == TILE_BY_COST)
         k_tile_cost<<<num_sms * 8, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, keys, ctl);
-    k_tile_hist<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, ctl);
+    k_tile_hist<<<num_sms * 4, TILE_ORDER_BLOCK, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist,
+                                                          ctl);
     k_tile_scan<<<1, TILE_SCAN_BLOCK, 0, st>>>(hist, ctl);
-    k_tile_scatter<<<num_sms * 4, 256, 0, st>>>(fo, head, dplus, tiles, count, seg, shift, mode, keys, hist, sorted,
-                                                ctl);
+    k_tile_scatter<<<num_sms * 4, TILE_ORDER_BLOCK, 0, st>>>(tiles, count, keys, hist, sorted, ctl);
 }
 
 void launch_prep(const u64* fo, u64 n, u64 nnz, u32* deg, u32* dplus, u64* cnt, u32* tile_i0, Control* ctl,
