@@ -41,6 +41,7 @@ WORKLOADS = {
     "rmat20": dict(kind="rmat", scale=20, edge_factor=16, seed=2),
     "rmat22": dict(kind="rmat", scale=22, edge_factor=16, seed=2),
     "rgg20": dict(kind="rgg2d", n=1 << 20, avg_degree=32.0, seed=3),
+    "rgg22": dict(kind="rgg2d", n=1 << 22, avg_degree=32.0, seed=3),
     # batched workload: many graphs, n log-uniform in [2^8, 2^17], degree U(4, 64),
     # G(n,m) / RMAT / RGG by index mod 3, graph i seeded with 4 + i
     "batch8192": dict(kind="batch", graphs=8192, log2_n=(8.0, 17.0), degree=(4.0, 64.0), seed=4),

@@ -162,7 +162,13 @@ ktri::Options resolve(const ktri_opts* o) {
 constexpr u64 HEAD_CHUNK_BYTES = u64(64) << 20;
 
 int ensure_chunk_events(ktri_ctx* ctx, size_t count) {
-    if (!ctx->copy_stream) KTRI_CK(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->copy_stream) {
+        // the pieces of head are copied by kernels that run beside the orientation of the pieces
+        // already in: the copy stream's blocks are dispatched first, so the copy keeps the link busy
+        int least = 0, greatest = 0;
+        KTRI_CK(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        KTRI_CK(ctx, cudaStreamCreateWithPriority(&ctx->copy_stream, cudaStreamNonBlocking, greatest));
+    }
     while (ctx->chunk_ev.size() < count) {
         cudaEvent_t e = nullptr;
         KTRI_CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

@@ -56,7 +56,9 @@ bool launch_copy(const void* src, void* dst, u64 bytes, int num_sms, cudaStream_
     }
     const u64 n16 = bytes / 16;
     u64 blocks = (n16 + 255) / 256;
-    const u64 cap = (u64)num_sms * 16;
+    // four blocks per SM (each with 16 KB of loads in flight) keep the link busy and leave room
+    // for kernels that run beside the copy
+    const u64 cap = (u64)num_sms * 4;
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     k_copy16<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16,

@@ -47,12 +47,15 @@ __global__ void k_prep(const u64* __restrict__ fo, u64 n, u64 nnz, u32* __restri
 // Orientation of one merge-path tile of W = 32 * IPT diagonals per warp.  The tile holds the
 // window vertices i0..i1 and the adjacency slots [j0, j1); every list with slots in the tile
 // has one piece there.  Slots are taken 32 at a time, one per lane, so the owner of a slot,
-// the rank of a kept entry among the tile's kept entries and a piece's count all come from
-// warp ballots and population counts: no block barrier, no per-thread path walk.
+// the rank of a kept entry among the tile's kept entries and the rank at a piece's ends all
+// come from warp ballots and population counts: no block barrier, no per-thread path walk.
+// Inside the tile all arithmetic is 32-bit (ids are below 2^32, slots relative to j0).
 //   vertex pass  at the slot where each piece starts: (window index + 1, degree of its vertex)
 //   pass 1       per slot: owner (the last piece start at or below the lane), deg[y] gather,
-//                the (deg, id) decision, input checks; at a piece's last slot its out-degree
-//                (a plain store, or an atomic reservation for a piece of a split list) and the
+//                the (deg, id) decision, input checks; the tile rank at each piece's first
+//                and past its last slot
+//   piece pass   per window vertex, lanes in parallel: the piece's out-degree share (a plain
+//                store, or an atomic reservation for a piece of a split list) and the
 //                gapped-array index of its first kept entry
 //   pass 2       kept entries written from registers, in slot order
 // A list held by one tile keeps its input order.  A split list's pieces reserve their ranges
@@ -68,7 +71,9 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     constexpr int WARPS = BLOCK / 32;
     constexpr u32 FULL = 0xFFFFFFFFu;
     __shared__ uint2 s_info_all[WARPS][W];  // at a piece's first slot: (window index + 1, degree)
-    __shared__ u64 s_base_all[WARPS][W];    // at a piece's first slot: headp index of tile rank 0
+    // at a piece's first slot: the tile ranks (at its first slot, past its last slot), then the
+    // headp index of tile rank 0 for its entries
+    __shared__ u64 s_base_all[WARPS][W];
 
     if (ctl->err & DEV_ERR_MASK) return;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -79,11 +84,13 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     const u64 d1 = d0 + W < total ? d0 + W : total;
     uint2* s_info = s_info_all[wid];
     u64* s_base = s_base_all[wid];
+    uint2* s_rank = reinterpret_cast<uint2*>(s_base);
     // tile_i0 holds base_tiles + 1 entries (the last is n), and tile + 1 <= base_tiles here
     const u64 i0 = tile_i0[tile], i1 = tile_i0[tile + 1];
     const u64 j0 = d0 - i0, j1 = d1 - i1;
     const u32 ns = (u32)(j1 - j0);
     if (ns == 0) return;  // only vertex ends: those lists have no slots here (out-degrees start at 0)
+    const u32 n32 = (u32)n;  // n < 2^32: every id fits
     // every slot's neighbour and its degree, all in flight before the window is read
     u32 y_r[IPT], dy_r[IPT];
 #pragma unroll
@@ -94,21 +101,19 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
 #pragma unroll
     for (int it = 0; it < IPT; ++it) {
         const u32 s = (u32)it * 32 + lane;
-        dy_r[it] = (s < ns && (u64)y_r[it] < n) ? __ldg(deg + y_r[it]) : 0u;
+        dy_r[it] = (s < ns && y_r[it] < n32) ? __ldg(deg + y_r[it]) : 0u;
     }
     for (u32 s = lane; s < ns; s += 32) s_info[s] = make_uint2(0u, 0u);
     __syncwarp();
     const u64 last_v = i1 < n ? i1 : n - 1;
     const u32 nwin = (u32)(last_v - i0) + 1;  // window vertices (at most W + 1)
-    u64 fo_i0;
-    {
-        // the first 32 window vertices with every lane present, so lane 0's start is shared
-        const bool have = (u32)lane < nwin;
-        const u64 a = have ? fo[i0 + lane] : 0, b = have ? fo[i0 + lane + 1] : 0;
-        fo_i0 = __shfl_sync(FULL, a, 0);
-        if (have && b > a && a < j1 && b > j0)
-            s_info[a > j0 ? a - j0 : 0] = make_uint2((u32)lane + 1, (u32)(b - a));
-    }
+    // the first 32 window vertices with every lane present (lane 0's list may begin before the
+    // tile); their bounds stay in registers for the piece pass
+    const bool have0 = (u32)lane < nwin;
+    const u64 a0 = have0 ? fo[i0 + lane] : 0, b0 = have0 ? fo[i0 + lane + 1] : 0;
+    const u64 fo_i0 = __shfl_sync(FULL, a0, 0), fo_i0_end = __shfl_sync(FULL, b0, 0);
+    if (have0 && b0 > a0 && a0 < j1 && b0 > j0)
+        s_info[a0 > j0 ? a0 - j0 : 0] = make_uint2((u32)lane + 1, (u32)(b0 - a0));
     for (u32 k = 32 + lane; k < nwin; k += 32) {
         const u64 v = i0 + k;
         const u64 a = fo[v], b = fo[v + 1];
@@ -116,13 +121,15 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
     }
     __syncwarp();
     const bool first_before = fo_i0 < j0;  // the first piece continues a list begun before the tile
+    // the first vertex's list continues past the tile
+    const bool first_past = fo_i0_end > j1;
     const u32 lt = (1u << lane) - 1u, le = lt | (1u << lane);
+    const u32 i0_32 = (u32)i0;
 
     u32 s0_r[IPT], km_r[IPT];
-    u32 rank = 0;                          // kept entries of the tile before this iteration
-    u32 s0c = 0, kc = 0, dc = 0, pc = 0;   // the piece open at the end of the previous iteration
-    u32 err = 0;
-    bool unsorted = false;
+    u32 rank = 0;                // kept entries of the tile before this iteration
+    u32 s0c = 0, kc = 0, dc = 0;  // the piece open at the end of the previous iteration
+    bool bad_id = false, self_loop = false, dup = false, unsorted = false;
 #pragma unroll
     for (int it = 0; it < IPT; ++it) {
         s0_r[it] = 0;
@@ -141,52 +148,65 @@ __global__ void __launch_bounds__(BLOCK) k_orient(const u64* __restrict__ fo, co
         const u32 k1 = here ? kx : kc;
         const u32 dx = here ? dxs : dc;
         const u32 y = y_r[it];
-        const u64 x = i0 + k1 - 1;
-        bool kept = false;
-        if (valid) {
-            if ((u64)y >= n) err |= DEV_ERR_ID_RANGE;
-            else if ((u64)y == x) err |= DEV_ERR_SELF_LOOP;
-            else kept = key_less(dx, x, dy_r[it], y);
-        }
+        const u32 x = i0_32 + k1 - 1;
+        const bool in_range = y < n32;
+        bad_id |= valid && !in_range;
+        self_loop |= valid && in_range && y == x;
+        const u32 dy = dy_r[it];
+        const bool kept = valid && in_range && y != x && (dx < dy || (dx == dy && x < y));
         const u32 km = __ballot_sync(FULL, kept);
-        const u32 pst = here ? rank + __popc(km & ((1u << (src & 31)) - 1u)) : pc;  // rank at the piece start
-        const u64 a = (k1 == 1 && first_before) ? fo_i0 : j0 + s0;
-        const u64 b = a + dx;
         const bool last_slot = s + 1 == ns;
         bool next_start;
         if (lane < 31) next_start = (starts >> (lane + 1)) & 1u;
         else next_start = valid && !last_slot && s_info[s + 1].x != 0;
-        // the next slot's neighbour: the next lane's, or lane 0's of the next iteration
+        // tile ranks at the piece's first slot and past its last slot
+        if (valid && info.x != 0) s_rank[s].x = rank + __popc(km & lt);
+        if (valid && (last_slot || next_start)) s_rank[s0].y = rank + __popc(km & le);
+        // the next slot's neighbour (the next lane's, or lane 0's of the next iteration) when it
+        // belongs to the same list: adjacent duplicates and order
         const u32 nd = __shfl_down_sync(FULL, y, 1);
         const u32 nn = __shfl_sync(FULL, y_r[it + 1 < IPT ? it + 1 : it], 0);
-        if (valid && (last_slot ? b > j1 : !next_start)) {
-            // the next slot holds the same list: adjacent duplicates and order
+        const bool past = (k1 == 1 && first_before) ? first_past : dx > ns - s0;
+        const bool same = valid && (last_slot ? past : !next_start);
+        if (same) {
             const u32 nx = last_slot ? __ldcs(head + j1) : (lane < 31 ? nd : nn);
-            if (nx < y) unsorted = true;
-            if (nx == y) err |= DEV_ERR_DUPLICATE;
-        }
-        if (valid && (last_slot || next_start)) {
-            // the piece's last slot in the tile: its out-degree share and its entries' place
-            const u32 cnt = rank + __popc(km & le) - pst;
-            u32 carry = 0;
-            if (a < j0 || b > j1) {
-                if (cnt) carry = atomicAdd(&dplus[x], cnt);
-                if (a >= j0) spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)x;
-            } else {
-                dplus[x] = cnt;
-            }
-            s_base[s0] = oriented_start(a, x) + carry - pst;
+            unsorted |= nx < y;
+            dup |= nx == y;
         }
         s0c = __shfl_sync(FULL, s0, 31);
         kc = __shfl_sync(FULL, k1, 31);
         dc = __shfl_sync(FULL, dx, 31);
-        pc = __shfl_sync(FULL, pst, 31);
         rank += __popc(km);
         s0_r[it] = s0;
         km_r[it] = km;
     }
+    const u32 err = (bad_id ? DEV_ERR_ID_RANGE : 0u) | (self_loop ? DEV_ERR_SELF_LOOP : 0u) |
+                    (dup ? DEV_ERR_DUPLICATE : 0u);
     if (err) atomicOr(&ctl->err, err);
     if (unsorted) atomicOr(&ctl->err, DEV_FLAG_UNSORTED);
+    __syncwarp();
+    // piece pass: out-degree shares and where each piece's kept entries go
+    {
+        auto settle = [&](u64 v, u64 a, u64 b) {
+            if (!(b > a && a < j1 && b > j0)) return;
+            const u32 s0 = a > j0 ? (u32)(a - j0) : 0u;
+            const uint2 rk = s_rank[s0];
+            const u32 cnt = rk.y - rk.x;
+            u32 carry = 0;
+            if (a < j0 || b > j1) {
+                if (cnt) carry = atomicAdd(&dplus[v], cnt);
+                if (a >= j0) spanning[atomicAdd(&ctl->spanning, 1ull)] = (u32)v;
+            } else {
+                dplus[v] = cnt;
+            }
+            s_base[s0] = oriented_start(a, v) + carry - rk.x;
+        };
+        if (have0) settle(i0 + lane, a0, b0);
+        for (u32 k = 32 + lane; k < nwin; k += 32) {
+            const u64 v = i0 + k;
+            settle(v, fo[v], fo[v + 1]);
+        }
+    }
     __syncwarp();
     rank = 0;
 #pragma unroll

@@ -455,6 +455,16 @@ void release_engine(ktri_server* s) {
     s->engine_launched = false;
 }
 
+// Copy between a slot's pinned staging (device-addressable) and its device buffers on st, by a
+// kernel: on Grace + Blackwell the copy engines have recurring slow windows that the SMs' own
+// loads and stores over the chip-to-chip link do not.  The copy engines take what a kernel
+// cannot (unaligned ends beyond 256 bytes).
+void copy_staging(const Slot& sl, void* dst, const void* src, size_t bytes, bool to_device, cudaStream_t st) {
+    if (bytes == 0) return;
+    if (!ktri::launch_copy(src, dst, bytes, ktri::ctx_num_sms(sl.ctx), st))
+        cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, st);
+}
+
 // Read-back of a counted batch on its slot's stream: totals, per-vertex counts (into pinned
 // staging, or straight into the callers' memory), then the slot's done event.
 int enqueue_readback(ktri_server* s, Slot& sl) {
@@ -463,7 +473,7 @@ int enqueue_readback(ktri_server* s, Slot& sl) {
     char* h = static_cast<char*>(sl.host);
     cudaStream_t st = sl.stream;
     const u64 k = sl.reqs.size(), n = sl.n_total;
-    cudaMemcpyAsync(h + sl.h_tot, d + sl.off_tot, 8 * k, cudaMemcpyDeviceToHost, st);
+    copy_staging(sl, h + sl.h_tot, d + sl.off_tot, 8 * k, false, st);
     if (sl.direct) {
         const u64 warps = (n + 255) / 256;
         const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
@@ -471,7 +481,7 @@ int enqueue_readback(ktri_server* s, Slot& sl) {
                                              reinterpret_cast<const u64*>(d + sl.off_vf), k, n,
                                              reinterpret_cast<const u64*>(d + sl.off_pv));
     } else {
-        cudaMemcpyAsync(h + sl.h_pv, d + sl.off_pv, 8 * n, cudaMemcpyDeviceToHost, st);
+        copy_staging(sl, h + sl.h_pv, d + sl.off_pv, 8 * n, false, st);
     }
     cudaEventRecord(sl.done, st);
     return cudaGetLastError() == cudaSuccess ? KTRI_OK : KTRI_ERR_CUDA;
@@ -545,10 +555,10 @@ int launch_batch(ktri_server* s, Slot& sl) {
     auto* dvf = reinterpret_cast<u64*>(d + sl.off_vf);
     auto* def = reinterpret_cast<u64*>(d + sl.off_ef);
     auto* dsrc = reinterpret_cast<GraphSrc*>(d + sl.off_src);
-    cudaMemcpyAsync(dvf, hvf, 8 * (k + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(def, hef, 8 * (k + 1), cudaMemcpyHostToDevice, st);
+    copy_staging(sl, dvf, hvf, 8 * (k + 1), true, st);
+    copy_staging(sl, def, hef, 8 * (k + 1), true, st);
     if (sl.direct) {
-        cudaMemcpyAsync(dsrc, hsrc, sizeof(GraphSrc) * k, cudaMemcpyHostToDevice, st);
+        copy_staging(sl, dsrc, hsrc, sizeof(GraphSrc) * k, true, st);
         const u64 warps = (std::max<u64>(n, nnz) + 255) / 256;
         const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
         k_gather<<<blocks, 256, 0, st>>>(dsrc, dvf, def, k, n, nnz, dfo, dhead);
@@ -581,8 +591,8 @@ int launch_batch(ktri_server* s, Slot& sl) {
 #pragma omp parallel for schedule(dynamic, 1) if (pieces.size() > 1 && nnz > (1u << 16))
         for (int64_t p = 0; p < (int64_t)pieces.size(); ++p)
             std::memcpy(pieces[(size_t)p].dst, pieces[(size_t)p].src, pieces[(size_t)p].bytes);
-        cudaMemcpyAsync(dfo, hfo, 8 * (n + 1), cudaMemcpyHostToDevice, st);
-        if (nnz) cudaMemcpyAsync(dhead, hhead, 4 * nnz, cudaMemcpyHostToDevice, st);
+        copy_staging(sl, dfo, hfo, 8 * (n + 1), true, st);
+        copy_staging(sl, dhead, hhead, 4 * nnz, true, st);
         const u64 warps = (std::max<u64>(n, nnz) + 255) / 256;
         const unsigned blocks = (unsigned)std::max<u64>(1, std::min<u64>((warps + 7) / 8, 152 * 16));
         k_rebase<<<blocks, 256, 0, st>>>(dfo, dhead, dvf, def, k, n, nnz);
