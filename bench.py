@@ -708,7 +708,9 @@ def main():
                      else "fallback 6.8 TB/s",
                      "algorithmic_bytes": b_int, "traffic": measured_traffic(args.workload),
                      "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum of the three counting kernels, one capture)"},
+                                       "dram__bytes_write.sum of the three counting kernels, captured at "
+                                       "RMAT-22 / RGG-22 and scaled by streamed entries; the RMAT-24 "
+                                       "figure is a lower bound, L2 reuse falls with size)"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(8 * (n + 1) + 4 * g.nnz), "d2h_bytes_per_step": int(8 * n + 8),
                 "call_wall_ms": {"min": min(walls), "median": statistics.median(walls), "max": max(walls),
