@@ -131,6 +131,10 @@ const char* ktri_version(void);
  * degree_outward, distributed_graph.h:148-163 and :538-566; sort_neighborhoods, :578-593)
  * and CetricEdgeIterator::run_local (include/cetric/counters/cetric_edge_iterator.h:173-227).
  * Host buffers in and out; copies to and from the device are part of the call; synchronous.
+ * Where the device can address a host buffer (pinned or registered memory, or pageable memory
+ * on platforms that let kernels address it, as Grace + Blackwell does) and its address is
+ * 16-byte aligned, the copy is done by the GPU's own loads and stores; otherwise by the copy
+ * engines.  Pinned, 16-byte-aligned buffers give the fastest calls.
  * per_vertex_out may be NULL; otherwise it receives n counts.  opts may be NULL.
  * Uses an internal context on the current CUDA device. */
 int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz, uint64_t* total_out,

@@ -579,8 +579,13 @@ __device__ __forceinline__ bool large_tile(unsigned char* smem, unsigned long lo
             // give the copy in flight a second bounded wait, so that it does not land in
             // shared memory after the block has left; then report the timeout (and, if the
             // copy still has not landed, that it may be in flight as the block leaves)
-            if (!__syncthreads_or(!mbar_wait_bounded(&s_bar, phase, COPY_WAIT_POLLS))) timed_out = true;
-            else timed_out = inflight = true;
+            if (!__syncthreads_or(!mbar_wait_bounded(&s_bar, phase, COPY_WAIT_POLLS))) {
+                timed_out = true;
+                phase ^= 1u;  // the copy landed: the barrier's phase completed (a block that goes on
+                              // taking tiles, as the engine's do, waits on the next one)
+            } else {
+                timed_out = inflight = true;
+            }
             break;
         }
         phase ^= 1u;
