@@ -975,7 +975,7 @@ __global__ void k_publish(EngineJob* job, unsigned long long seq, const u64* fo,
 }
 
 __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words,
-                                                         const unsigned* stop, u32 idle_polls) {
+                                                         unsigned* stop, u32 idle_polls) {
     constexpr int BLOCK = ENGINE_BLOCK;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_job;
@@ -983,6 +983,7 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
     __shared__ EngineJob s_jb;  // the claimed job's record, read at L2 by thread 0
     __shared__ u32 s_jb_slot;
     __shared__ unsigned s_stop;
+    __shared__ int s_work;  // some published job was unfinished in the last scan
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     (void)lane;
     // the large-owner tiles' bulk-copy barrier: outside the dynamic region, which the small- and
@@ -1002,13 +1003,17 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
     while (true) {
         if (threadIdx.x == 0) {
             s_job = -1;
+            s_work = 0;
+            // a launch leaves as a whole: once any block has set the stop word (or the host has),
+            // no block claims another unit
             s_stop = *(volatile const unsigned*)stop;
-            for (u32 k = 0; k < njobs && s_job < 0; ++k) {
+            for (u32 k = 0; k < njobs && s_job < 0 && !s_stop; ++k) {
                 const u32 j = (start + k) % njobs;
                 volatile EngineJob* vj = jobs + j;
                 for (int attempt = 0; attempt < 4; ++attempt) {
                     const unsigned long long s1 = vj->seq;
                     if (s1 == 0) break;
+                    s_work = 1;  // a published job is not finished
                     __threadfence();
                     const unsigned long long cur = vj->next;
                     const unsigned long long units = vj->units;
@@ -1045,7 +1050,20 @@ __global__ void __launch_bounds__(ENGINE_BLOCK, 4) k_engine(EngineJob* jobs, u32
         __syncthreads();
         const int j = s_job;
         if (j < 0) {
-            if (++idle > idle_polls || s_stop) break;  // the same decision in every thread
+            // Only scans that found every published job finished count towards leaving: while a
+            // job's last units run on other blocks, this block stays for the jobs published next.
+            // The first block to leave sets the stop word, and the others follow at their next
+            // scan: a launch that shrank to a few blocks would serve a job published meanwhile at
+            // a trickle, and the host relaunches the engine only once the launch has ended.
+            if (s_work) idle = 0;
+            if (s_stop) break;  // the same decision in every thread
+            if (++idle > idle_polls) {
+                if (threadIdx.x == 0) {
+                    *(volatile unsigned*)stop = 1u;
+                    __threadfence();
+                }
+                break;
+            }
             __nanosleep(2000);
             __syncthreads();  // every thread has read s_job before thread 0 writes it again
             continue;
@@ -1117,11 +1135,14 @@ int engine_grid(int num_sms) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_engine, ENGINE_BLOCK, ENGINE_SMEM);
         occ = o > 0 ? o : 1;
     }
-    // leave room on every SM for the preparation kernels of the batches being published
-    return num_sms * (occ > 1 ? occ - 1 : 1);
+    // leave room on every SM for the preparation kernels of the batches being published: the
+    // engine's blocks stay resident while any published job is unfinished, so with one block
+    // slot per SM left the next batches' orientation starved (6.4K against 0.6-2.5K graphs/s at
+    // saturation with two slots left against one)
+    return num_sms * (occ > 2 ? occ - 2 : 1);
 }
 
-void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, const unsigned* stop, u32 idle_polls,
+void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, unsigned* stop, u32 idle_polls,
                    int grid, cudaStream_t st) {
     k_engine<<<grid, ENGINE_BLOCK, ENGINE_SMEM, st>>>(jobs, njobs, done_words, stop, idle_polls);
 }

@@ -158,12 +158,14 @@ constexpr u32 ENGINE_UNIT_ITEMS = ENGINE_BLOCK / 32 * ENGINE_REPS;  // vertex ba
 void launch_publish(EngineJob* job, unsigned long long seq, const u64* fo, const u32* head, u64 n,
                     const void* vdesc, const u32* headp, const uint2* mtiles, const uint2* ltiles, u64* cnt,
                     Control* ctl, u32 small_d, u32 seg, unsigned long long* done_word, cudaStream_t st);
-// The engine: blocks drain published jobs and leave after idle_polls empty scans (about 2 us
-// each) or when *stop is nonzero.  done_words[j] (host-mapped) receives job j's sequence number
-// when its last unit is done.
+// The engine: blocks drain published jobs.  A block that has made idle_polls scans (about 2 us
+// each) finding every published job finished sets *stop and leaves; every block leaves at its
+// next scan once *stop is nonzero (set by a block or by the host), so a launch ends as a whole.
+// *stop must be 0 when the engine is launched.  done_words[j] (host-mapped) receives job j's
+// sequence number when its last unit is done.
 int engine_grid(int num_sms);
 size_t engine_smem_bytes();
-void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, const unsigned* stop, u32 idle_polls,
+void launch_engine(EngineJob* jobs, u32 njobs, unsigned long long* done_words, unsigned* stop, u32 idle_polls,
                    int grid, cudaStream_t st);
 
 // u64 ids (the binary file format) -> u32 ids; ids above 2^32 - 1 become 0xFFFFFFFF.

@@ -91,6 +91,9 @@ __global__ void k_rebase(u64* __restrict__ fo, u32* __restrict__ head, const u64
     }
 }
 
+// One word written by one thread (the engine's stop word, from a stream of its own).
+__global__ void k_set_word(unsigned* p, unsigned v) { *(volatile unsigned*)p = v; }
+
 __global__ void k_gather(const GraphSrc* __restrict__ src, const u64* __restrict__ vf, const u64* __restrict__ ef,
                          u64 k, u64 n, u64 nnz, u64* __restrict__ dfo, u32* __restrict__ dhead) {
     const int lane = threadIdx.x & 31;
@@ -239,7 +242,8 @@ struct ktri_server {
     ktri::EngineJob* jobs = nullptr;         // device, one per slot
     unsigned long long* done_host = nullptr;  // host-mapped completion words, one per slot
     unsigned long long* done_dev = nullptr;   // their device address
-    unsigned* stop_dev = nullptr;             // device flag: 1 tells the engine to leave
+    unsigned* stop_dev = nullptr;             // device word: nonzero tells the engine to leave
+    cudaStream_t control_stream = nullptr;    // highest priority: sets stop_dev while the engine runs
     cudaStream_t engine_stream = nullptr;
     cudaEvent_t engine_done = nullptr;        // recorded after each engine launch
     bool engine_launched = false;
@@ -415,6 +419,8 @@ SlotLayout slot_layout(u64 n, u64 nnz, u64 k, bool direct) {
 
 // Pack the slot's requests and launch their count.  Called without the lock.
 // Engine scans without a published job before an engine launch leaves (about 2 us each).
+// Scans with every published job finished (about 2 us each) before the engine leaves; it leaves
+// as a whole (the first block to go sets the stop word).
 constexpr unsigned ENGINE_IDLE_POLLS = 100;
 
 size_t slot_index(const ktri_server* s, const Slot& sl) { return (size_t)(&sl - s->slots.data()); }
@@ -428,6 +434,7 @@ int ensure_engine(ktri_server* s) {
         if (q == cudaErrorNotReady) return KTRI_OK;
         if (q != cudaSuccess) return KTRI_ERR_CUDA;
     }
+    k_set_word<<<1, 1, 0, s->engine_stream>>>(s->stop_dev, 0u);  // before the launch, in stream order
     ktri::launch_engine(s->jobs, (u32)s->slots.size(), s->done_dev, s->stop_dev, ENGINE_IDLE_POLLS, s->engine_grid,
                         s->engine_stream);
     cudaEventRecord(s->engine_done, s->engine_stream);
@@ -439,18 +446,20 @@ int ensure_engine(ktri_server* s) {
 // Tell a running engine to leave, wait for it, and free its resources (the worker has ended).
 void release_engine(ktri_server* s) {
     if (s->engine_launched && s->stop_dev) {
-        cudaMemsetAsync(s->stop_dev, 0xFF, sizeof(unsigned), s->aux);
+        k_set_word<<<1, 1, 0, s->control_stream>>>(s->stop_dev, 1u);
         cudaStreamSynchronize(s->engine_stream);
     }
     if (s->engine_done) cudaEventDestroy(s->engine_done);
     if (s->engine_stream) cudaStreamDestroy(s->engine_stream);
-    if (s->jobs) cudaFree(s->jobs);
+    if (s->control_stream) cudaStreamDestroy(s->control_stream);
     if (s->stop_dev) cudaFree(s->stop_dev);
+    if (s->jobs) cudaFree(s->jobs);
     if (s->done_host) cudaFreeHost(s->done_host);
     s->engine_done = nullptr;
     s->engine_stream = nullptr;
     s->jobs = nullptr;
     s->stop_dev = nullptr;
+    s->control_stream = nullptr;
     s->done_host = nullptr;
     s->engine_launched = false;
 }
@@ -854,13 +863,17 @@ int ktri_server_create(int device, const ktri_server_opts* opts, ktri_server** o
     }
     cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
     if (rc == KTRI_OK && s->engine) {
-        // job records (zero: nothing published), the host-mapped completion words and the stop flag
+        // job records (zero: nothing published), the host-mapped completion words, the stop word
+        // and the highest-priority stream that sets it while the engine runs
         void* hp = nullptr;
+        int least_prio = 0, greatest_prio = 0;
         if (cudaMalloc(&s->jobs, sizeof(ktri::EngineJob) * s->slots.size()) != cudaSuccess ||
             cudaMalloc(&s->stop_dev, sizeof(unsigned)) != cudaSuccess ||
             cudaHostAlloc(&hp, sizeof(unsigned long long) * s->slots.size(), cudaHostAllocMapped) != cudaSuccess ||
             cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->done_dev), hp, 0) != cudaSuccess ||
             cudaStreamCreateWithFlags(&s->engine_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&s->control_stream, cudaStreamNonBlocking, greatest_prio) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->engine_done, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
             rc = KTRI_ERR_CUDA;
