@@ -31,7 +31,7 @@ extern "C" {
 #define KTRI_ERR_OUT_OF_MEMORY (-3)    /* device or host allocation failed, or over the memory budget */
 #define KTRI_ERR_CUDA (-4)             /* a CUDA runtime call failed; see ktri_last_error */
 #define KTRI_ERR_TIMEOUT (-5)          /* a bounded device-side wait gave up */
-#define KTRI_ERR_UNSUPPORTED (-6)      /* valid input outside what this build handles */
+#define KTRI_ERR_UNSUPPORTED (-6)      /* valid input outside what the library handles */
 #define KTRI_ERR_IO (-7)               /* file could not be read or written, or is malformed */
 #define KTRI_ERR_NO_DEVICE (-8)        /* no CUDA device, or the requested one does not exist */
 

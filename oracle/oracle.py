@@ -3,8 +3,8 @@
 The oracle restates KaTric's shared-memory local counting path (orientation by
 (degree, id), per-vertex id sort, node-parallel edge iterator with the four
 intersection strategies).  Only tests/, ``__graft_entry__.smoke()`` and
-``bench.py``'s CPU-baseline leg use it, always as the checker or the timed CPU
-baseline, never as the product path.
+``bench.py``'s CPU-baseline leg use it, always as the reference the GPU results are
+compared with or as the timed CPU baseline, never as the product path.
 """
 from __future__ import annotations
 
