@@ -417,8 +417,6 @@ SlotLayout slot_layout(u64 n, u64 nnz, u64 k, bool direct) {
     return L;
 }
 
-// Pack the slot's requests and launch their count.  Called without the lock.
-// Engine scans without a published job before an engine launch leaves (about 2 us each).
 // Scans with every published job finished (about 2 us each) before the engine leaves; it leaves
 // as a whole (the first block to go sets the stop word).
 constexpr unsigned ENGINE_IDLE_POLLS = 100;
@@ -506,6 +504,7 @@ int finish_engine_batch(ktri_server* s, Slot& sl) {
     return enqueue_readback(s, sl);
 }
 
+// Pack the slot's requests and launch their count.  Called without the lock.
 int launch_batch(ktri_server* s, Slot& sl) {
     const u64 k = sl.reqs.size();
     u64 n = 0, nnz = 0;
