@@ -70,27 +70,6 @@ __device__ __forceinline__ Desc<u64> load_desc<u64>(const Desc<u64>* p) {
 // Total order of the orientation, node_ordering::degree_outward: (deg, id).
 __device__ __forceinline__ bool key_less(u64 da, u64 a, u64 db, u64 b) { return da < db || (da == db && a < b); }
 
-// Merge-path search over the merged sequence of vertex-end events (first_out[1..n]) and
-// adjacency slots (0..nnz): the largest i in [0, n] with first_out[i] + i <= d.  The
-// point (i, d - i) is where diagonal d crosses the path.
-__device__ __forceinline__ u64 mp_search(const u64* __restrict__ fo, u64 n, u64 d) {
-    u64 lo = 0, hi = n < d ? n : d;
-    while (lo < hi) {
-        u64 mid = (lo + hi + 1) >> 1;
-        if (__ldg(fo + mid) + mid <= d) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Same search inside a shared-memory window s_fo[k] = first_out[base + k], i in [lo, hi].
-__device__ __forceinline__ u64 mp_search_window(const u64* s_fo, u64 base, u64 lo, u64 hi, u64 d) {
-    while (lo < hi) {
-        u64 mid = (lo + hi + 1) >> 1;
-        if (s_fo[mid - base] + mid <= d) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
 // Exclusive block-wide scan of one u32 per thread.  s_warp holds BLOCK/32 entries.
 // Contains __syncthreads(); every thread of the block must call it.
 template <int BLOCK>
