@@ -134,7 +134,9 @@ const char* ktri_version(void);
  * Where the device can address a host buffer (pinned or registered memory, or pageable memory
  * on platforms that let kernels address it, as Grace + Blackwell does) and its address is
  * 16-byte aligned, the copy is done by the GPU's own loads and stores; otherwise by the copy
- * engines.  Pinned, 16-byte-aligned buffers give the fastest calls.
+ * engines.  A read-back of 1 MiB or more into pageable memory is staged in the context's pinned
+ * buffer and copied by host threads after the call's synchronisation.  Pinned, 16-byte-aligned
+ * buffers give the fastest calls.
  * per_vertex_out may be NULL; otherwise it receives n counts.  opts may be NULL.
  * Uses an internal context on the current CUDA device. */
 int ktri_count_csr(const uint64_t* first_out, const uint32_t* head, uint64_t n, uint64_t nnz, uint64_t* total_out,
