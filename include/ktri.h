@@ -299,7 +299,10 @@ int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_
  * memory budget and counts it on one of `slots` contexts, while batches already on the GPU
  * keep running (their work overlaps).  Counted graphs stay resident (CSR and counts on the
  * device, keyed by graph_key) until the budget needs their room; a request for a resident
- * key is answered from the resident counts.  submit copies the caller's CSR, or with
+ * key is answered from the resident counts (the per-vertex counts are also kept in host
+ * memory, up to a quarter of memory_budget in all, so a repeat needs no device copy).  submit
+ * checks first_out (0 first, nnz last, non-decreasing: KTRI_ERR_INVALID_CSR otherwise) and
+ * copies the caller's CSR, or with
  * KTRI_SUBMIT_BORROW reads it in place (the caller keeps it alive and unchanged until wait
  * returns); first_out may be NULL to repeat a key that is resident, queued or counting.  A
  * request whose key is queued or counting (same n and nnz) joins that count instead of

@@ -184,6 +184,9 @@ struct Resident {  // a graph kept on the device with its counts
     void* mem = nullptr;  // [fo u64 n+1][head u32 nnz][pv u64 n]
     size_t bytes = 0;
     std::list<uint64_t>::iterator lru;
+    // the per-vertex counts on the host as well (read-only, shared with every request that a
+    // cache hit answers), while the server's host copies stay within a quarter of the budget
+    std::shared_ptr<std::vector<uint64_t>> pv_host;
 };
 
 struct Slot {
@@ -234,6 +237,7 @@ struct ktri_server {
     std::unordered_map<uint64_t, Request*> leaders;  // key -> the queued or counting request for it
     std::list<uint64_t> lru;  // front = most recent
     size_t resident_bytes = 0;
+    size_t host_pv_bytes = 0;  // host bytes of the resident graphs' pv_host
     ktri_server_stats st{};
     int fatal = KTRI_OK;
     double alloc_s_acc = 0;  // seconds spent in grow() by the worker, moved into st.alloc_us under the lock
@@ -271,6 +275,7 @@ bool make_room(ktri_server* s, size_t need, size_t inflight) {
         if (it != s->resident.end()) {
             cudaFreeAsync(it->second.mem, s->aux);
             s->resident_bytes -= it->second.bytes;
+            if (it->second.pv_host) s->host_pv_bytes -= 8 * it->second.n;
             s->resident.erase(it);
             s->st.evictions++;
         }
@@ -299,14 +304,25 @@ void finish(ktri_server* s, Request* r, int status) {
 }
 
 // Answer a request for a resident graph from its resident counts.
+// Host copies of resident counts are kept while they total at most a quarter of the budget.
+bool host_pv_room(const ktri_server* s, u64 n) { return s->host_pv_bytes + 8 * n <= s->opts.memory_budget / 4; }
+
 void serve_resident(ktri_server* s, Request* r, Resident& res) {
     r->total = res.total;
     if (r->want_pv && res.n) {
-        r->pv = std::make_shared<std::vector<uint64_t>>(res.n);
-        const char* base = static_cast<const char*>(res.mem);
-        const size_t off_pv = al(8 * (res.n + 1)) + al(4 * (res.nnz + 1));
-        cudaMemcpyAsync(r->pv->data(), base + off_pv, 8 * res.n, cudaMemcpyDeviceToHost, s->aux);
-        cudaStreamSynchronize(s->aux);
+        if (res.pv_host) {
+            r->pv = res.pv_host;  // no copy under the lock: the request shares the host counts
+        } else {
+            r->pv = std::make_shared<std::vector<uint64_t>>(res.n);
+            const char* base = static_cast<const char*>(res.mem);
+            const size_t off_pv = al(8 * (res.n + 1)) + al(4 * (res.nnz + 1));
+            cudaMemcpyAsync(r->pv->data(), base + off_pv, 8 * res.n, cudaMemcpyDeviceToHost, s->aux);
+            cudaStreamSynchronize(s->aux);
+            if (host_pv_room(s, res.n)) {
+                res.pv_host = r->pv;
+                s->host_pv_bytes += 8 * res.n;
+            }
+        }
     }
     s->lru.erase(res.lru);
     s->lru.push_front(res.key);
@@ -345,6 +361,10 @@ void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 eb
     res.total = r->total;
     res.mem = mem;
     res.bytes = bytes;
+    if (r->pv && r->pv->size() == r->n && r->n && host_pv_room(s, r->n)) {
+        res.pv_host = r->pv;
+        s->host_pv_bytes += 8 * r->n;
+    }
     s->lru.push_front(r->key);
     res.lru = s->lru.begin();
     s->resident_bytes += bytes;
@@ -811,6 +831,37 @@ void worker_main(ktri_server* s) {
     }
 }
 
+// first_out[0..n] is non-decreasing.  Blocks of offsets are tested without early exits (a loop
+// the compiler vectorises), the blocks of a large graph by several threads: a submit checks
+// every offset of its graph, which for the largest graphs of a stream costs more than the rest
+// of the request.
+bool offsets_nondecreasing(const uint64_t* fo, uint64_t n) {
+    constexpr uint64_t BLK = uint64_t(1) << 14;
+    const int64_t blocks = (int64_t)((n + BLK - 1) / BLK);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad) if (n >= (uint64_t(1) << 18))
+    for (int64_t b = 0; b < blocks; ++b) {
+        const uint64_t v0 = (uint64_t)b * BLK, v1 = std::min(n, v0 + BLK);
+        int acc = 0;
+        for (uint64_t v = v0; v < v1; ++v) acc |= fo[v + 1] < fo[v] ? 1 : 0;
+        bad |= acc;
+    }
+    return bad == 0;
+}
+
+// Copy of a request's per-vertex counts into the caller's buffer, in 4 MiB pieces by several
+// threads for a large graph.
+void copy_counts(uint64_t* dst, const uint64_t* src, uint64_t n) {
+    constexpr size_t PIECE = size_t(4) << 20;
+    const size_t bytes = 8 * n;
+    const int64_t pieces = (int64_t)((bytes + PIECE - 1) / PIECE);
+#pragma omp parallel for schedule(static) if (pieces > 1)
+    for (int64_t p = 0; p < pieces; ++p) {
+        const size_t o = (size_t)p * PIECE;
+        std::memcpy(reinterpret_cast<char*>(dst) + o, reinterpret_cast<const char*>(src) + o, std::min(PIECE, bytes - o));
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -923,8 +974,7 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     if (first_out) {
         if (n > 0x7FFFFFFFull) return KTRI_ERR_UNSUPPORTED;
         if (first_out[0] != 0 || first_out[n] != nnz || (nnz && !head)) return KTRI_ERR_INVALID_CSR;
-        for (uint64_t v = 0; v < n; ++v)
-            if (first_out[v + 1] < first_out[v]) return KTRI_ERR_INVALID_CSR;
+        if (!offsets_nondecreasing(first_out, n)) return KTRI_ERR_INVALID_CSR;
         r->n = n;
         r->nnz = nnz;
         if (flags & KTRI_SUBMIT_BORROW) {
@@ -998,7 +1048,7 @@ int ktri_server_wait(ktri_server* s, uint64_t request_id, uint64_t* total, uint6
     if (status == KTRI_OK) {
         if (total) *total = r->total;
         if (per_vertex_out && r->want_pv && r->n) {
-            if (r->pv) std::memcpy(per_vertex_out, r->pv->data(), 8 * r->n);
+            if (r->pv) copy_counts(per_vertex_out, r->pv->data(), r->n);
             else std::memset(per_vertex_out, 0, 8 * r->n);
         }
     }

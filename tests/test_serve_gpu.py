@@ -111,6 +111,32 @@ def test_repeats_while_queued_join_the_count(direct):
             assert total == w[0] and np.array_equal(pv, w[1])
 
 
+def test_submit_checks_offsets_and_repeats_share_the_host_counts():
+    """A submit refuses a graph whose offsets decrease, for a graph large enough that several
+    threads check its offsets and for a small one.  A graph counted without per-vertex counts
+    answers its first repeat that wants them from the device copy and later repeats from the
+    host copy kept with it; every answer equals the plain count."""
+    g = Graph.rmat(18, 8, seed=5)
+    small = graph_mix(4, seed=3)[1]
+    with TriangleCounter(0) as ctr:
+        want = ctr.count(g.first_out, g.head)
+    with Server(slots=2) as srv:
+        for base in (g, small):
+            bad = base.first_out.copy()
+            k = base.n // 2
+            bad[k] = bad[k + 1] + 1  # one offset above its successor; first and last stay valid
+            with pytest.raises(KtriError) as e:
+                srv.submit(Graph(bad, base.head), key=0)
+            assert e.value.code == _native.ERR_INVALID_CSR
+        total, pv, _ = srv.wait(srv.submit(g, key=9, per_vertex=False))
+        assert total == want[0] and pv is None
+        for _ in range(3):
+            total, pv, _ = srv.wait(srv.submit(None, key=9))
+            assert total == want[0] and np.array_equal(pv, want[1])
+            pv[:] = 0  # the caller's copy: later answers do not see it
+        assert srv.stats()["cache_hits"] == 3
+
+
 def test_engine_folds_arrivals_into_the_running_kernel():
     """Requests that arrive while the engine counts are prepared on a free slot and published
     to the running engine: many batches, fewer engine launches, every result exact.  After the
