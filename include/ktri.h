@@ -300,7 +300,9 @@ int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_
  * keep running (their work overlaps).  Counted graphs stay resident (CSR and counts on the
  * device, keyed by graph_key) until the budget needs their room; a request for a resident
  * key is answered from the resident counts (the per-vertex counts are also kept in host
- * memory, up to a quarter of memory_budget in all, so a repeat needs no device copy).  submit
+ * memory, up to a quarter of memory_budget in all, so a repeat needs no device copy).  A key
+ * names one graph: a graph of another n or nnz submitted under a resident key is counted and
+ * replaces the resident one.  submit
  * checks first_out (0 first, nnz last, non-decreasing: KTRI_ERR_INVALID_CSR otherwise) and
  * copies the caller's CSR, or with
  * KTRI_SUBMIT_BORROW reads it in place (the caller keeps it alive and unchanged until wait

@@ -225,7 +225,8 @@ struct ktri_server {
     ktri_server_opts opts{};
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<Request*> pending;
+    std::deque<Request*> pending;  // requests to count, in arrival order
+    std::deque<Request*> hits;     // requests for keys resident at submit: answered from them
     std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
     uint64_t next_id = 1;
     bool stop = false;
@@ -265,20 +266,23 @@ size_t batch_bytes(u64 n, u64 nnz, u64 k) {
            (size_t)ktri_workspace_bytes(n, nnz, KTRI_METHOD_AUTO);
 }
 
+// Drop one resident graph (called with s->mu held).
+void drop_resident(ktri_server* s, std::unordered_map<uint64_t, Resident>::iterator it) {
+    cudaFreeAsync(it->second.mem, s->aux);
+    s->resident_bytes -= it->second.bytes;
+    if (it->second.pv_host) s->host_pv_bytes -= 8 * it->second.n;
+    s->lru.erase(it->second.lru);
+    s->resident.erase(it);
+    s->st.evictions++;
+}
+
 // Evict least-recently-used resident graphs until `need` more bytes fit the budget.
 // Called with s->mu held.
 bool make_room(ktri_server* s, size_t need, size_t inflight) {
     while (s->resident_bytes + inflight + need > s->opts.memory_budget && !s->lru.empty()) {
-        const uint64_t key = s->lru.back();
-        s->lru.pop_back();
-        auto it = s->resident.find(key);
-        if (it != s->resident.end()) {
-            cudaFreeAsync(it->second.mem, s->aux);
-            s->resident_bytes -= it->second.bytes;
-            if (it->second.pv_host) s->host_pv_bytes -= 8 * it->second.n;
-            s->resident.erase(it);
-            s->st.evictions++;
-        }
+        auto it = s->resident.find(s->lru.back());
+        if (it != s->resident.end()) drop_resident(s, it);
+        else s->lru.pop_back();
     }
     return s->resident_bytes + inflight + need <= s->opts.memory_budget;
 }
@@ -334,7 +338,13 @@ void serve_resident(ktri_server* s, Request* r, Resident& res) {
 // taken on the device from the slot's union, on the auxiliary stream, which the slot's next
 // batch waits for (cache_done) before it overwrites the union.
 void keep_resident(ktri_server* s, Request* r, const Slot& sl, u64 vbase, u64 ebase, size_t inflight) {
-    if (!r->key || s->resident.count(r->key)) return;
+    if (!r->key) return;
+    // a key names one graph: a graph of another size counted under a resident key replaces it
+    auto old = s->resident.find(r->key);
+    if (old != s->resident.end()) {
+        if (old->second.n == r->n && old->second.nnz == r->nnz) return;
+        drop_resident(s, old);
+    }
     const size_t bytes = al(8 * (r->n + 1)) + al(4 * (r->nnz + 1)) + al(8 * (r->n + 1));
     if (bytes > s->opts.memory_budget / 4) return;
     if (!make_room(s, bytes, inflight)) return;
@@ -751,23 +761,23 @@ void worker_main(ktri_server* s) {
             }
             any_busy |= sl.busy;
         }
-        if (s->stop && s->pending.empty() && !any_busy) break;
-        // requests for resident graphs are answered at once
-        for (auto it = s->pending.begin(); it != s->pending.end();) {
-            Request* r = *it;
-            auto res = r->key ? s->resident.find(r->key) : s->resident.end();
-            if (res != s->resident.end()) {
+        if (s->stop && s->pending.empty() && s->hits.empty() && !any_busy) break;
+        // requests for keys that were resident when submitted are answered at once (a graph of
+        // another size under the key, or a key evicted since, is counted if its CSR came along)
+        while (!s->hits.empty()) {
+            Request* r = s->hits.front();
+            s->hits.pop_front();
+            auto res = s->resident.find(r->key);
+            if (res != s->resident.end() && r->n == res->second.n && r->nnz == res->second.nnz) {
                 serve_resident(s, r, res->second);
                 finish(s, r, KTRI_OK);
-                it = s->pending.erase(it);
-                s->cv_done.notify_all();
-            } else if (!r->bfo) {  // a repeat by key of a graph that is no longer resident
+            } else if (r->bfo) {
+                s->pending.push_back(r);
+                continue;
+            } else {  // a repeat by key of a graph that is no longer resident (or was replaced)
                 finish(s, r, KTRI_ERR_INVALID_ARGUMENT);
-                it = s->pending.erase(it);
-                s->cv_done.notify_all();
-            } else {
-                ++it;
             }
+            s->cv_done.notify_all();
         }
         // admit a batch into a free slot
         Slot* free_slot = nullptr;
@@ -1022,7 +1032,7 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     r->t_submit = now_s();
     *request_id = r->id;
     if (graph_key && !resident && lead == s->leaders.end()) s->leaders[graph_key] = r.get();
-    s->pending.push_back(r.get());
+    (resident ? s->hits : s->pending).push_back(r.get());
     s->requests.emplace(r->id, std::move(r));
     s->st.submitted++;
     s->cv_work.notify_one();

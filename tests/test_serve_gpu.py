@@ -115,11 +115,13 @@ def test_submit_checks_offsets_and_repeats_share_the_host_counts():
     """A submit refuses a graph whose offsets decrease, for a graph large enough that several
     threads check its offsets and for a small one.  A graph counted without per-vertex counts
     answers its first repeat that wants them from the device copy and later repeats from the
-    host copy kept with it; every answer equals the plain count."""
+    host copy kept with it.  A key names one graph: a graph of another size under a resident
+    key is counted and replaces it.  Every answer equals the plain count."""
     g = Graph.rmat(18, 8, seed=5)
-    small = graph_mix(4, seed=3)[1]
+    small, other = graph_mix(4, seed=3)[1:3]
     with TriangleCounter(0) as ctr:
         want = ctr.count(g.first_out, g.head)
+        want_other = ctr.count(other.first_out, other.head)
     with Server(slots=2) as srv:
         for base in (g, small):
             bad = base.first_out.copy()
@@ -135,6 +137,15 @@ def test_submit_checks_offsets_and_repeats_share_the_host_counts():
             assert total == want[0] and np.array_equal(pv, want[1])
             pv[:] = 0  # the caller's copy: later answers do not see it
         assert srv.stats()["cache_hits"] == 3
+        # a graph of another size under the same key is counted (not answered from the resident
+        # graph) and replaces it: a repeat by key then answers for the new graph
+        assert other.n != g.n
+        for _ in range(2):
+            total, pv, _ = srv.wait(srv.submit(other, key=9))
+            assert total == want_other[0] and np.array_equal(pv, want_other[1])
+        total, pv, _ = srv.wait(srv.submit(None, key=9))
+        assert total == want_other[0] and np.array_equal(pv, want_other[1])
+        assert srv.stats()["cache_hits"] == 5
 
 
 def test_engine_folds_arrivals_into_the_running_kernel():
