@@ -302,14 +302,15 @@ int ktri_autotune(ktri_ctx* ctx, const uint64_t* d_first_out, const uint32_t* d_
  * key is answered from the resident counts (the per-vertex counts are also kept in host
  * memory, up to a quarter of memory_budget in all, so a repeat needs no device copy).  A key
  * names one graph: a graph of another n or nnz submitted under a resident key is counted and
- * replaces the resident one.  submit
- * checks first_out (0 first, nnz last, non-decreasing: KTRI_ERR_INVALID_CSR otherwise) and
- * copies the caller's CSR, or with
- * KTRI_SUBMIT_BORROW reads it in place (the caller keeps it alive and unchanged until wait
- * returns); first_out may be NULL to repeat a key that is resident, queued or counting.  A
+ * replaces the resident one.  submit checks first_out (0 first, nnz last, non-decreasing:
+ * KTRI_ERR_INVALID_CSR otherwise) and copies the caller's CSR, or with KTRI_SUBMIT_BORROW
+ * reads it in place (the caller keeps it alive and unchanged until wait returns).  first_out
+ * may be NULL to repeat a key that is resident, queued or counting, with n = 0 (any size) or
+ * the vertex count that the caller's per-vertex buffer holds: a repeat whose key's graph has
+ * another n fails with KTRI_ERR_INVALID_ARGUMENT instead of writing past that buffer.  A
  * request whose key is queued or counting (same n and nnz) joins that count instead of
- * starting another.  wait blocks until the request is done and reports its latency (submit to
- * completion). */
+ * starting another.  wait blocks until the request is done and reports its latency (submit
+ * to completion). */
 #define KTRI_SUBMIT_PER_VERTEX 1u /* return per-vertex counts */
 #define KTRI_SUBMIT_BORROW 2u     /* read the caller's CSR in place instead of copying it */
 typedef struct ktri_server ktri_server;

@@ -768,13 +768,14 @@ void worker_main(ktri_server* s) {
             Request* r = s->hits.front();
             s->hits.pop_front();
             auto res = s->resident.find(r->key);
-            if (res != s->resident.end() && r->n == res->second.n && r->nnz == res->second.nnz) {
+            if (res != s->resident.end() && r->n == res->second.n && (!r->bfo || r->nnz == res->second.nnz)) {
+                r->nnz = res->second.nnz;
                 serve_resident(s, r, res->second);
                 finish(s, r, KTRI_OK);
             } else if (r->bfo) {
                 s->pending.push_back(r);
                 continue;
-            } else {  // a repeat by key of a graph that is no longer resident (or was replaced)
+            } else {  // a repeat by key of a graph that is no longer resident, or of another size
                 finish(s, r, KTRI_ERR_INVALID_ARGUMENT);
             }
             s->cv_done.notify_all();
@@ -1004,7 +1005,9 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     const bool resident = graph_key && s->resident.count(graph_key);
     auto lead = graph_key && !resident ? s->leaders.find(graph_key) : s->leaders.end();
     // a request for a key that is queued or counting joins that count (same graph size only)
-    if (lead != s->leaders.end() && (!first_out || (lead->second->n == n && lead->second->nnz == nnz))) {
+    // (a repeat without a CSR may name the vertex count it expects in n: 0 takes any)
+    if (lead != s->leaders.end() && (!first_out ? (n == 0 || lead->second->n == n)
+                                                : (lead->second->n == n && lead->second->nnz == nnz))) {
         Request* l = lead->second;
         r->n = l->n;
         r->nnz = l->nnz;
@@ -1025,7 +1028,7 @@ int ktri_server_submit(ktri_server* s, uint64_t graph_key, const uint64_t* first
     if (!first_out && !resident) return KTRI_ERR_INVALID_ARGUMENT;
     if (!first_out) {
         const Resident& res = s->resident.at(graph_key);
-        r->n = res.n;
+        r->n = n ? n : res.n;  // checked against the resident graph when the worker answers
         r->nnz = res.nnz;
     }
     r->id = s->next_id++;

@@ -44,8 +44,14 @@ class Server:
         if graph is None:
             if not key:
                 raise ValueError("a repeat needs the key of a resident graph")
-            rc = self._L.ktri_server_submit(self._h, key, None, None, 0, 0, flags & 1, ctypes.byref(rid))
             n = self._sizes.get(key, 0)
+            if per_vertex and not n and key not in self._sizes:
+                raise ValueError("a repeat with per-vertex counts needs a key this Server was given a graph for")
+            # n: the vertex count the counts buffer is sized for; the server refuses the request
+            # (KTRI_ERR_INVALID_ARGUMENT) if the graph resident under the key has another (n = 0
+            # would take any size, so a graph without vertices is repeated without counts)
+            rc = self._L.ktri_server_submit(self._h, key, None, None, n, 0, flags & 1 if n else 0,
+                                            ctypes.byref(rid))
         else:
             rc = self._L.ktri_server_submit(self._h, key, graph.first_out.ctypes.data,
                                             graph.head.ctypes.data if graph.nnz else None, graph.n, graph.nnz,

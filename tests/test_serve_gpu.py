@@ -2,6 +2,7 @@
 the mix, repeats are answered from resident graphs, the memory budget is honoured, and with
 the engine batches published while the persistent counting kernel runs are counted by that
 same kernel."""
+import ctypes
 import threading
 import time
 
@@ -146,6 +147,15 @@ def test_submit_checks_offsets_and_repeats_share_the_host_counts():
         total, pv, _ = srv.wait(srv.submit(None, key=9))
         assert total == want_other[0] and np.array_equal(pv, want_other[1])
         assert srv.stats()["cache_hits"] == 5
+        # a repeat without a CSR that names another vertex count than the resident graph's is
+        # refused (its counts buffer would be too small), one that names none takes any size
+        L = _native.load()
+        for expect_n, want_rc in ((g.n, _native.ERR_INVALID_ARGUMENT), (0, 0)):
+            rid = ctypes.c_uint64(0)
+            _native.check(L.ktri_server_submit(srv._h, 9, None, None, expect_n, 0, 0, ctypes.byref(rid)))
+            total = ctypes.c_uint64(0)
+            assert L.ktri_server_wait(srv._h, rid.value, ctypes.byref(total), None, None) == want_rc
+            assert want_rc or total.value == want_other[0]
 
 
 def test_engine_folds_arrivals_into_the_running_kernel():
